@@ -1,0 +1,194 @@
+"""ctypes loader for the FP64 CPU oracle (oracle/liboracle.so).
+
+TEST INFRASTRUCTURE ONLY.  The test suite, the smoke check and the
+CPU-baseline leg of ``bench.py`` import this module as the checker; the
+product (the CUDA library and the ``annmap`` package) never does.
+
+The oracle restates the reference's CPU map path; see oracle.h for the file
+and line of the reference each function follows.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+import threading
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB = None
+_LOCK = threading.Lock()
+
+
+class OrcHpx(C.Structure):
+    _fields_ = [("nside", C.c_int64), ("npix", C.c_int64), ("ncap", C.c_int64),
+                ("fact1", C.c_double), ("fact2", C.c_double)]
+
+
+class OrcParams(C.Structure):
+    _fields_ = [
+        ("h100", C.c_double), ("Omega_M", C.c_double), ("Lbox_in_Mpc", C.c_double),
+        ("mass_to_Msun", C.c_double), ("redshift", C.c_double),
+        ("centerpos", C.c_double * 3), ("obs_pos", C.c_double * 3),
+        ("align_vec", C.c_double * 3), ("particle_masses", C.c_double * 10),
+        ("nside", C.c_int),
+        ("rho_crit_in_cgs", C.c_double), ("length_to_cgs", C.c_double),
+        ("mass_to_cgs", C.c_double), ("density_to_cgs", C.c_double),
+        ("time_to_cgs", C.c_double), ("velocity_to_cgs", C.c_double),
+        ("annihilation_flux_to_cgs", C.c_double),
+        ("otheta", C.c_double), ("ophi", C.c_double),
+        ("rotmatrix", (C.c_double * 3) * 3),
+        ("unit_factor", C.c_double), ("hires_threshold", C.c_double),
+        ("npix", C.c_int64), ("dOmega", C.c_double), ("theta0", C.c_double),
+    ]
+
+
+class OrcStats(C.Structure):
+    _fields_ = [("kept", C.c_int64), ("skipped", C.c_int64),
+                ("single_small", C.c_int64), ("single_disc", C.c_int64),
+                ("disc", C.c_int64), ("deposits", C.c_int64)]
+
+
+def build(force: bool = False) -> str:
+    """Compile liboracle.so with the committed Makefile (gcc, seconds)."""
+    so = os.path.join(HERE, "liboracle.so")
+    srcs = [os.path.join(HERE, f) for f in ("healpix_ring.c", "annmap_oracle.c", "oracle.h")]
+    stale = (not os.path.exists(so)) or any(os.path.getmtime(s) > os.path.getmtime(so) for s in srcs)
+    if force or stale:
+        subprocess.run(["make", "-s", "-C", HERE, "liboracle.so"], check=True)
+    return so
+
+
+def lib():
+    global _LIB
+    with _LOCK:
+        if _LIB is None:
+            L = C.CDLL(build())
+            P = C.POINTER
+            f32 = P(C.c_float)
+            L.orc_hpx_init.argtypes = [P(OrcHpx), C.c_int64]
+            L.orc_hpx_ang2pix.argtypes = [P(OrcHpx), C.c_double, C.c_double]
+            L.orc_hpx_ang2pix.restype = C.c_int64
+            L.orc_hpx_pix2vec.argtypes = [P(OrcHpx), C.c_int64, P(C.c_double)]
+            L.orc_hpx_pix2ang.argtypes = [P(OrcHpx), C.c_int64, P(C.c_double), P(C.c_double)]
+            L.orc_hpx_ring_above.argtypes = [P(OrcHpx), C.c_double]
+            L.orc_hpx_ring_above.restype = C.c_int64
+            L.orc_hpx_ring2z.argtypes = [P(OrcHpx), C.c_int64]
+            L.orc_hpx_ring2z.restype = C.c_double
+            L.orc_hpx_ring_info.argtypes = [P(OrcHpx), C.c_int64, P(C.c_int64), P(C.c_int64), P(C.c_int)]
+            L.orc_hpx_query_disc.argtypes = [P(OrcHpx), C.c_double, C.c_double, C.c_double,
+                                             P(C.c_int64), P(C.c_int64)]
+            L.orc_hpx_query_disc.restype = C.c_int64
+            L.orc_hpx_query_disc_list.argtypes = [P(OrcHpx), C.c_double, C.c_double, C.c_double,
+                                                  P(C.c_int32)]
+            L.orc_hpx_query_disc_list.restype = C.c_int64
+            L.orc_params_setup.argtypes = [P(OrcParams)]
+            L.orc_render.argtypes = [P(OrcParams), f32, f32, f32, f32, f32, f32, C.c_int64,
+                                     P(C.c_double), P(OrcStats), C.c_int]
+            L.orc_render.restype = C.c_int
+            L.orc_finalize.argtypes = [P(OrcParams), P(C.c_double)]
+            L.orc_finalize.restype = C.c_double
+            L.orc_particle_geom.argtypes = [P(OrcParams), C.c_float, C.c_float, C.c_float,
+                                            C.c_float, C.c_float, C.c_float, P(C.c_double)]
+            _LIB = L
+    return _LIB
+
+
+# ---------------------------------------------------------------- HEALPix
+class Healpix:
+    """RING-scheme HEALPix functions of the oracle (FP64)."""
+
+    def __init__(self, nside: int):
+        self.b = OrcHpx()
+        lib().orc_hpx_init(C.byref(self.b), nside)
+        self.nside, self.npix = nside, 12 * nside * nside
+
+    def ang2pix(self, theta, phi):
+        return lib().orc_hpx_ang2pix(C.byref(self.b), float(theta), float(phi))
+
+    def pix2vec(self, pix):
+        v = (C.c_double * 3)()
+        lib().orc_hpx_pix2vec(C.byref(self.b), int(pix), v)
+        return np.array(v[:])
+
+    def pix2ang(self, pix):
+        t, p = C.c_double(), C.c_double()
+        lib().orc_hpx_pix2ang(C.byref(self.b), int(pix), C.byref(t), C.byref(p))
+        return t.value, p.value
+
+    def ring_above(self, z):
+        return lib().orc_hpx_ring_above(C.byref(self.b), float(z))
+
+    def ring2z(self, ring):
+        return lib().orc_hpx_ring2z(C.byref(self.b), int(ring))
+
+    def ring_info(self, ring):
+        s, n, sh = C.c_int64(), C.c_int64(), C.c_int()
+        lib().orc_hpx_ring_info(C.byref(self.b), int(ring), C.byref(s), C.byref(n), C.byref(sh))
+        return s.value, n.value, bool(sh.value)
+
+    def query_disc(self, theta, phi, radius) -> np.ndarray:
+        tot = C.c_int64()
+        lib().orc_hpx_query_disc(C.byref(self.b), float(theta), float(phi), float(radius), None,
+                                 C.byref(tot))
+        out = np.empty(max(tot.value, 1), dtype=np.int32)
+        n = lib().orc_hpx_query_disc_list(C.byref(self.b), float(theta), float(phi), float(radius),
+                                          out.ctypes.data_as(C.POINTER(C.c_int32)))
+        return out[:n]
+
+
+# ---------------------------------------------------------------- params
+def make_params(*, nside, obs_pos, centerpos, align_vec, h100=0.73, Omega_M=0.238,
+                Lbox_in_Mpc=0.001, mass_to_Msun=1.0, particle_masses=(0.0,),
+                redshift=0.0) -> OrcParams:
+    p = OrcParams()
+    p.h100, p.Omega_M, p.Lbox_in_Mpc, p.mass_to_Msun, p.redshift = (
+        h100, Omega_M, Lbox_in_Mpc, mass_to_Msun, redshift)
+    for i in range(3):
+        p.centerpos[i], p.obs_pos[i], p.align_vec[i] = centerpos[i], obs_pos[i], align_vec[i]
+    for i in range(10):
+        p.particle_masses[i] = particle_masses[i] if i < len(particle_masses) else 0.0
+    p.nside = int(nside)
+    lib().orc_params_setup(C.byref(p))
+    return p
+
+
+def rotmatrix(p: OrcParams) -> np.ndarray:
+    return np.array([[p.rotmatrix[i][j] for j in range(3)] for i in range(3)])
+
+
+# ---------------------------------------------------------------- map
+def _f32(a):
+    a = np.ascontiguousarray(a, dtype=np.float32)
+    return a, a.ctypes.data_as(C.POINTER(C.c_float))
+
+
+def render(p: OrcParams, parts: dict, nthreads: int = 1, finalize: bool = True):
+    """Runs the restated CPU map loop.  ``parts`` holds float32 arrays
+    x, y, z, m, rho, h.  Returns (map, stats, totalC)."""
+    keep = []
+    ptrs = []
+    for k in ("m", "rho", "h", "x", "y", "z"):
+        a, ptr = _f32(parts[k])
+        keep.append(a)
+        ptrs.append(ptr)
+    n = len(keep[0])
+    mp = np.zeros(int(p.npix), dtype=np.float64)
+    st = OrcStats()
+    rc = lib().orc_render(C.byref(p), *ptrs, n, mp.ctypes.data_as(C.POINTER(C.c_double)),
+                          C.byref(st), int(nthreads))
+    if rc != 0:
+        raise RuntimeError("oracle render failed")
+    total = None
+    if finalize:
+        total = lib().orc_finalize(C.byref(p), mp.ctypes.data_as(C.POINTER(C.c_double)))
+    stats = {k: getattr(st, k) for k, _ in OrcStats._fields_}
+    return mp, stats, total
+
+
+def particle_geom(p: OrcParams, m, rho, h, x, y, z) -> dict:
+    out = (C.c_double * 8)()
+    lib().orc_particle_geom(C.byref(p), m, rho, h, x, y, z, out)
+    keys = ("d", "flux", "costheta", "phi", "theta", "ar", "pix", "kept")
+    return dict(zip(keys, out[:]))

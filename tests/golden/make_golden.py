@@ -1,0 +1,148 @@
+"""Generates the golden fixtures in tests/golden/ from the reference's own
+CPU map path.
+
+The reference's src/genmap.cpp, src/parameters.cpp, src/anglefuncs.cpp,
+src/datatypes.cpp, src/datareader.cpp and src/flux/flux_ann_nosom.cpp are
+compiled where they lie by oracle/ref_shim/Makefile (HEALPix and XDR replaced
+by stand-ins; see that directory) into oracle/_ref/annmap_ref.  For each case
+below this script writes the reference's own inputs -- an info file and a
+native particle file (int32 N + N x 48-byte DMParticle records, plus an
+optional byte mask file) -- runs the reference binary, and stores the inputs,
+the info file text, the derived Parameters fields and the output map in
+``<case>.npz``.
+
+Run here (the reference sources are only present on this machine):
+    python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import os
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, os.path.join(REPO, "dm-annihilation-cxx_gb300", "pywrapper"))
+from annmap import synth  # noqa: E402
+
+REF_BIN = os.path.join(REPO, "oracle", "_ref", "annmap_ref")
+
+
+def build_ref():
+    subprocess.run(["make", "-s", "-C", os.path.join(REPO, "oracle", "ref_shim")], check=True)
+
+
+def write_native(path, P, extra_mass=None):
+    rec = np.zeros((len(P), 12), np.float32)
+    rec[:, 0] = P.m if extra_mass is None else extra_mass
+    rec[:, 1] = P.rho
+    rec[:, 2] = P.h
+    rec[:, 3] = P.x
+    rec[:, 4] = P.y
+    rec[:, 5] = P.z
+    with open(path, "wb") as f:
+        np.array([len(P)], np.int32).tofile(f)
+        rec.tofile(f)
+    return rec
+
+
+def parse_params(text):
+    out = {}
+    for line in text.strip().splitlines():
+        k, *v = line.split()
+        out[k] = np.array([float(x) for x in v])
+    return out
+
+
+def run_case(name, P, *, nside, info_extra="", mass=None, mask=None, particle_masses=None,
+             obs=None, centre=(0.0, 0.0, 0.0), align=(0.0, 0.0, 1.0), units="kpc",
+             mem_buffer=1000, test=None):
+    d = tempfile.mkdtemp(prefix="golden_")
+    rec = write_native(os.path.join(d, "parts.bin"), P, extra_mass=mass)
+    obs = P.obs_pos if obs is None else obs
+    pm = particle_masses if particle_masses is not None else [P.particle_mass]
+    lines = ["# golden case " + name, "Omega_M = 0.238", "h100 = 0.73", "n_s = 0.951",
+             "sigma_8 = 0.74"]
+    if units == "kpc":
+        lines += ["Lbox_in_Mpc = 0.001", "mass_to_Msun = 1"]
+    else:  # the reference's own Via Lactea II unit system: mass derived from rho_crit * L^3
+        lines += ["Lbox_in_Mpc = 40.0"]
+    lines += ["particle_masses = " + " ".join(repr(float(x)) for x in pm),
+              "centerpos = " + " ".join(repr(float(x)) for x in centre),
+              "align_vec = " + " ".join(repr(float(x)) for x in align),
+              "obs_pos = " + " ".join(repr(float(x)) for x in obs),
+              f"nside = {nside}", f"mem_buffer = {mem_buffer}",
+              f"datafile = {d}/parts.bin"]
+    if test is not None:
+        lines.append(f"test = {test}")
+    if mask is not None:
+        with open(os.path.join(d, "mask.bin"), "wb") as f:
+            np.array([len(P)], np.int32).tofile(f)
+            np.asarray(mask, np.uint8).tofile(f)
+        lines.append(f"mask = {d}/mask.bin")
+    lines.append("outputmap = unused.fits")
+    ini = "\n".join(lines) + "\n" + info_extra
+    with open(os.path.join(d, "info.ini"), "w") as f:
+        f.write(ini)
+    r = subprocess.run([REF_BIN, os.path.join(d, "info.ini"), os.path.join(d, "map.bin"),
+                        os.path.join(d, "par.txt")], capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"{name}: reference failed: {r.stderr[-500:]}")
+    mp = np.fromfile(os.path.join(d, "map.bin"), np.float64)
+    with open(os.path.join(d, "par.txt")) as f:
+        par = parse_params(f.read())
+    np.savez_compressed(
+        os.path.join(HERE, name + ".npz"), map=mp, info=np.array(ini.replace(d, "@DIR@")),
+        records=rec, mask=(np.asarray(mask, np.uint8) if mask is not None else np.zeros(0, np.uint8)),
+        **{"par_" + k: v for k, v in par.items()})
+    assert np.all(np.isfinite(mp)), name
+    print(f"{name}: nside={nside} n={len(P)} sum(map*dOmega)={mp.sum() * par['dOmega'][0]:.6e}")
+
+
+def main():
+    build_ref()
+    os.makedirs(HERE, exist_ok=True)
+    # 1. small NFW host, generic observer, Nside 16
+    run_case("nfw_ns16", synth.nfw_halo(400, seed=101), nside=16)
+    # 2. host + subhalos, Nside 64, chunked reading (mem_buffer < N)
+    run_case("nfw_sub_ns64", synth.nfw_halo(3000, seed=102, n_sub=8), nside=64, mem_buffer=700)
+    # 3. near-observer particles (discs past pi: all-sky) + far tiny particles
+    P = synth.nfw_halo(600, seed=103, near_observer=40, near_radius=0.5)
+    run_case("near_observer_ns32", P, nside=32)
+    # 4. observer on the z axis (polar frame) and on the x axis
+    P = synth.nfw_halo(500, seed=104, obs_pos=(0.0, 0.0, 8.0))
+    run_case("obs_zaxis_ns32", P, nside=32)
+    P = synth.nfw_halo(500, seed=105, obs_pos=(8.0, 0.0, 0.0))
+    run_case("obs_xaxis_ns32", P, nside=32, align=(0.3, -0.2, 0.93))
+    # 5. two mass resolutions (the hires filter) and a mask (dens = -1)
+    P = synth.nfw_halo(1500, seed=106)
+    rng = np.random.Generator(np.random.PCG64(1106))
+    mass = P.m.copy()
+    heavy = rng.uniform(size=len(P)) < 0.3
+    mass[heavy] = P.particle_mass * 8.0
+    mask = (rng.uniform(size=len(P)) > 0.2).astype(np.uint8)
+    run_case("hires_mask_ns32", P, nside=32, mass=mass, mask=mask,
+             particle_masses=[P.particle_mass * 8.0, P.particle_mass])
+    # 6. the reference's own unit system (Lbox 40 Mpc, mass from rho_crit L^3),
+    #    positions in box units around a VL2-like centre, test limit
+    P = synth.nfw_halo(800, seed=107)
+    c = np.array([0.3612030, 0.2106580, 0.00687726])
+    scale = 1.0 / 40000.0  # kpc -> box units of 40 Mpc
+    Q = synth.Particles((P.x * scale + c[0]).astype(np.float32), (P.y * scale + c[1]).astype(np.float32),
+                        (P.z * scale + c[2]).astype(np.float32), (P.m * 1e-12).astype(np.float32),
+                        P.rho, (P.h * scale).astype(np.float32))
+    obs = tuple((np.array(P.obs_pos) * scale + c).tolist())
+    run_case("vl2units_ns16", Q, nside=16, units="vl2", particle_masses=[4.1e-9],
+             obs=obs, centre=tuple(c.tolist()), align=(-0.025836, 0.133297, 0.990739), test=700)
+    # 7. a non power of two Nside and high-resolution small discs (single-pixel branches)
+    P = synth.nfw_halo(2000, seed=108, n_sub=4)
+    run_case("nside24", P, nside=24)
+    P = synth.nfw_halo(1200, seed=109, n_sub=30, sub_frac=0.6)
+    run_case("subhalo_ns128", P, nside=128)
+
+
+if __name__ == "__main__":
+    main()
