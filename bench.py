@@ -1,0 +1,354 @@
+"""Benchmark of the annihilation sky-map projection on GB300.
+
+Headline metric (the benchmark spec): particles/s at Nside 2048 for the
+compensated-FP32 form, with the plain FP64-accumulate GPU form and the
+per-pixel error against FP64 reported beside it.  Workload: the 16,777,216-
+particle NFW host + 100 subhalos set (seeded synthetic stand-in for the
+reference's simulation data), one observer at 8 kpc, HEALPix Nside 2048.
+
+A step renders the whole particle set into one map.  ``value`` times steps
+with inputs resident in HBM; ``e2e`` times the public API with pinned host
+inputs and a host map (H2D of the particles and D2H of the 403 MB map inside
+every step).  Inputs (403 MB) plus the map and accumulation planes (805 MB)
+exceed the 126 MB L2, so no explicit L2 flush is done between steps.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(REPO, "dm-annihilation-cxx_gb300", "pywrapper"))
+
+import numpy as np  # noqa: E402
+
+METRIC = "particles/s at Nside 2048: comp-FP32 vs plain GPU form; px err vs FP64"
+UNIT = "particles/s"
+WORKLOAD = "nfw16m_sub100_ns2048"
+KERNELS_PER_STEP = 6  # prep, key scan, queue scatter, disc (block), disc (warp), finalize
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default=WORKLOAD)
+    ap.add_argument("--scale", type=float, default=1.0, help="fraction of the workload's particles")
+    ap.add_argument("--plain-scale", type=float, default=1.0 / 64)
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--no-extras", action="store_true", help="skip plain form, e2e and CPU legs")
+    return ap.parse_args()
+
+
+def dist_init(args):
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch.distributed as dist
+        backend = "nccl" if args.impl == "gb300" else "gloo"
+        dist.init_process_group(backend=backend)
+    return ws, rank, local
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def allmax(ws, v, device=None):
+    if ws == 1:
+        return v
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([v], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.t.join(timeout=2)
+
+    def summary(self):
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 8:
+                continue
+            try:
+                sm.append(float(f[0]))
+                smax.append(float(f[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[4:8]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        busy = [s for s in sm if s > 0.5 * max(sm)] or sm
+        return {"sm_mhz": statistics.median(busy), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    p = os.path.join(REPO, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return d.get("hbm_gbs", 6800.0), "measured"
+    return 6800.0, "fallback"
+
+
+def profile_traffic():
+    """Per-launch DRAM bytes of the disc kernels from the committed ncu summary."""
+    p = os.path.join(REPO, "profiles", "disc_comp_traffic.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            return json.load(f)
+    return None
+
+
+def rel_err(got, ref):
+    mask = ref > 1e-6 * ref.max()
+    r = np.abs(got[mask] - ref[mask]) / ref[mask]
+    return float(np.median(r)), float(r.max())
+
+
+def cpu_oracle_run(P, nside, seconds, threads=None):
+    """Times the FP64 oracle (CPU restatement of the reference map path) on a
+    bounded prefix of the (shuffled, hence i.i.d.) particle set."""
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import oracle as O
+    threads = threads or os.cpu_count() or 1
+    o = O.make_params(nside=nside, obs_pos=P.obs_pos, centerpos=P.centerpos, align_vec=P.align_vec,
+                      particle_masses=(P.particle_mass,))
+    # calibrate on a small prefix, then size the sample to ~`seconds`
+    n0 = min(len(P), 64 * threads)
+    t0 = time.perf_counter()
+    O.render(o, P.subset(slice(0, n0)).as_dict(), nthreads=threads, finalize=False)
+    dt0 = max(time.perf_counter() - t0, 1e-3)
+    n = int(min(len(P), max(n0, n0 * seconds / dt0)))
+    sub = P.subset(slice(0, n))
+    t0 = time.perf_counter()
+    mp, st, tot = O.render(o, sub.as_dict(), nthreads=threads)
+    dt = time.perf_counter() - t0
+    return {"value": n / dt, "unit": UNIT, "cores": threads, "seconds": dt, "particles": n,
+            "deposits": st["deposits"]}, sub, mp, tot
+
+
+def run_reference(args, ws, rank):
+    """The reference arm: the CPU restatement of the reference's own map path
+    (src/genmap.cpp) timed on this host's cores on the same workload."""
+    if rank != 0:
+        return
+    from annmap import synth
+    P, nside = synth.workload(args.workload, scale=args.scale)
+    threads = os.cpu_count() or 1
+    per_step = max(2.0, min(20.0, 150.0 / max(1, args.steps + args.warmup)))
+    vals = []
+    info = None
+    for i in range(args.warmup + args.steps):
+        info, _, _, _ = cpu_oracle_run(P.subset(slice(i * 0, None)), nside, per_step, threads)
+        if i >= args.warmup:
+            vals.append(info["value"])
+    v = statistics.median(vals)
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * len(P) / v,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded NFW host + subhalos)",
+            "config": {"workload": args.workload, "particles": len(P), "nside": nside,
+                       "form": "reference CPU map path (FP64), restated"},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": f"{info['particles']} of {len(P)} particles per step "
+                                       f"(shuffled prefix, i.i.d.), all {threads} host threads"},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_gb300(args, ws, rank, local):
+    import torch
+    import annmap
+    from annmap import synth
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    P, nside = synth.workload(args.workload, scale=args.scale)
+    n = len(P)
+    npix = 12 * nside * nside
+    par = annmap.Parameters.for_synthetic(P, nside)
+    host = P.as_dict()
+    dparts = {k: torch.from_numpy(v).to(dev) for k, v in host.items()}
+    dmap = torch.zeros(npix, dtype=torch.float64, device=dev)
+    r = annmap.Renderer(local)
+    r.set_params(par)
+    stream = torch.cuda.current_stream(dev)
+    r.set_stream(stream)
+
+    for _ in range(args.warmup):
+        r.render(dparts, nside, annmap.COMP_F32, out=dmap)
+    torch.cuda.synchronize()
+    disc_ms, step_stats = [], None
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        barrier(ws)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(args.steps):
+            r.render(dparts, nside, annmap.COMP_F32, out=dmap)
+            step_stats = r.stats()
+            disc_ms.append(step_stats["disc_ms"])
+        e1.record(stream)
+        torch.cuda.synchronize()
+        barrier(ws)
+    ms = e0.elapsed_time(e1) / args.steps
+    ms = allmax(ws, ms, dev)
+    value = ws * n / (ms / 1e3)
+    clocks = clk.summary()
+    comp_map = dmap.cpu().numpy()
+
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded NFW host + 100 subhalos; reference data unavailable)",
+            "config": {"workload": args.workload, "particles": n, "nside": nside,
+                       "form": "compensated FP32 (FP64 geometry, FP32 weights, two-float sums)",
+                       "parallelism": f"replicas x{ws}",
+                       "l2": "no flush: inputs 403 MB + map/planes 805 MB > 126 MB L2"},
+            "clocks": clocks, "gpu_launches": KERNELS_PER_STEP * args.steps,
+            "deposits_per_step": step_stats["deposits"],
+            "deposits_per_s": step_stats["deposits"] / (ms / 1e3),
+            "stage_ms": {"step": ms, "disc_kernels": statistics.mean(disc_ms)}}
+
+    # roofline of the dominant kernels (the disc kernels): one 8-byte
+    # read-modify-write reduction per algorithmic deposit
+    peak, peak_src = measured_peaks()
+    dms = statistics.mean(disc_ms)
+    alg_bytes = 8.0 * step_stats["deposits"]
+    achieved = alg_bytes / (dms / 1e3) / 1e9
+    traffic = profile_traffic()
+    line["roofline"] = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                        "frac": achieved / peak, "peak_source": peak_src,
+                        "traffic": traffic["dram_bytes_per_launch_scaled"] if traffic else None,
+                        "algorithmic_bytes": alg_bytes,
+                        "basis": "8 B per deposit (FP64 map read-modify-write) / disc-kernel time"}
+
+    if not args.no_extras and rank == 0:
+        # plain FP64 form on a prefix (the plain form is FP64-throughput bound)
+        k = max(1024, int(n * args.plain_scale))
+        sub = {kk: v[:k] for kk, v in dparts.items()}
+        pmap = torch.zeros_like(dmap)
+        cmap = torch.zeros_like(dmap)
+        r.render(sub, nside, annmap.PLAIN_F64, out=pmap)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        r.render(sub, nside, annmap.PLAIN_F64, out=pmap)
+        torch.cuda.synchronize()
+        tp = time.perf_counter() - t0
+        pst = r.stats()
+        r.render(sub, nside, annmap.COMP_F32, out=cmap)
+        cst = r.stats()
+        torch.cuda.synchronize()
+        pm, cm = pmap.cpu().numpy(), cmap.cpu().numpy()
+        med, mx = rel_err(cm, pm)
+        plain_value = k / tp
+        line["plain_form"] = {"value": plain_value, "unit": UNIT, "particles": k,
+                              "ms_per_step": tp * 1e3, "disc_ms": pst["disc_ms"]}
+        line["speedup_vs_plain"] = value / ws / plain_value
+        line["px_err"] = {"vs": "GPU plain FP64 form, same particles", "particles": k,
+                          "median": med, "max": mx, "floor": "pixels > 1e-6 max",
+                          "total_flux_rel": abs(cm.sum() - pm.sum()) / pm.sum(),
+                          "nonzero_sets_equal": bool(np.array_equal(cm != 0, pm != 0))}
+        # e2e through the public API: pinned host inputs -> host map
+        pin = {kk: torch.from_numpy(v).pin_memory() for kk, v in host.items()}
+        hmap = torch.zeros(npix, dtype=torch.float64).pin_memory()
+        hmap_np = hmap.numpy()
+        r.set_stream(None)
+        r.render({kk: v.numpy() for kk, v in pin.items()}, nside, annmap.COMP_F32, out=hmap_np)
+        ke = max(1, min(args.steps, 3))
+        t0 = time.perf_counter()
+        for _ in range(ke):
+            r.render({kk: v.numpy() for kk, v in pin.items()}, nside, annmap.COMP_F32, out=hmap_np)
+        te = (time.perf_counter() - t0) / ke
+        line["e2e"] = {"value": n / te, "unit": UNIT, "h2d_bytes_per_step": 24 * n,
+                       "d2h_bytes_per_step": 8 * npix, "ms_per_step": te * 1e3, "steps": ke}
+        dev_vs_host = rel_err(hmap_np, comp_map)
+        line["e2e"]["max_rel_diff_vs_device_run"] = dev_vs_host[1]
+        # CPU baseline (rank 0, N = 1): the oracle on a bounded sample, and
+        # the GPU map of the same sample against it
+        if ws == 1:
+            cpu, csub, omap, otot = cpu_oracle_run(P, nside, args.cpu_seconds)
+            line["cpu_baseline"] = {"value": cpu["value"], "unit": UNIT, "cores": cpu["cores"],
+                                    "kind": "port",
+                                    "sample": f"{cpu['particles']} of {n} particles (shuffled prefix, "
+                                              f"i.i.d.), {cpu['seconds']:.1f} s on {cpu['cores']} threads"}
+            r.set_stream(None)
+            g = r.render(csub.as_dict(), nside, annmap.COMP_F32)
+            med2, mx2 = rel_err(g, omap)
+            dom = 4 * math.pi / npix
+            line["px_err_vs_oracle"] = {"particles": cpu["particles"], "median": med2, "max": mx2,
+                                        "total_flux_rel": abs(g.sum() * dom - otot) / otot}
+    r.close()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    ws, rank, local = dist_init(args)
+    if args.impl == "reference":
+        run_reference(args, ws, rank)
+    else:
+        run_gb300(args, ws, rank, local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

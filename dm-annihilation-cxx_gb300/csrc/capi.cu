@@ -1,0 +1,537 @@
+// capi.cu -- the C ABI (include/dmann.h): contexts, device workspace, ring
+// tables and the render pipeline
+//   prep (geometry, filter, single-pixel deposits, size/sky keys)
+//   -> key scan -> queue scatter (largest discs first)
+//   -> disc kernels (block per large disc, warp per small disc)
+//   -> final map pass (divide by dOmega, optional accumulate).
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/dmann.h"
+#include "frame.h"
+#include "kernels.cuh"
+
+using namespace dmann;
+
+namespace {
+
+struct DevBuf {
+    void *p = nullptr;
+    size_t bytes = 0;
+};
+
+struct RingTables {
+    double *z = nullptr, *st = nullptr, *theta = nullptr;
+};
+
+}  // namespace
+
+struct dmann_ctx {
+    int device = 0;
+    int num_sms = 0;
+    cudaStream_t own = nullptr;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr, evd0 = nullptr, evd1 = nullptr;
+    bool disc_timed = false;
+    bool have_frame = false, have_units = false;
+    double rot[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
+    double opos[3] = {0, 0, 0};
+    double unit_factor = 1.0, hires = INFINITY;
+    int flux_model = DMANN_FLUX_ANN_NOSOM;
+    dmann_tuning tune{};
+    std::map<int, RingTables> rings;
+    // workspace
+    DevBuf in[6], theta, phi, ar, flux, cpix, key, queue, hist, ctr, fsum, acc, map;
+    dmann_stats stats{};
+    bool stats_pending = false;
+    long long *h_ctr = nullptr;   // pinned: C_COUNT counters + the flux sum
+    double *h_fsum = nullptr;
+    // the map being accumulated (dmann_map_begin .. dmann_map_end)
+    Hpx g{};
+    RingTables rt;
+    int precision = DMANN_COMP_F32;
+    bool in_map = false;
+    std::string err;
+};
+
+namespace {
+
+dmann_status fail(dmann_ctx *c, dmann_status s, const std::string &msg) {
+    if (c) c->err = msg;
+    return s;
+}
+
+#define CK(call)                                                                                  \
+    do {                                                                                          \
+        cudaError_t e_ = (call);                                                                  \
+        if (e_ != cudaSuccess)                                                                    \
+            return fail(ctx, DMANN_ERR_CUDA,                                                      \
+                        std::string(#call) + ": " + cudaGetErrorString(e_));                      \
+    } while (0)
+
+dmann_status ensure(dmann_ctx *ctx, DevBuf &b, size_t bytes) {
+    if (b.bytes >= bytes) return DMANN_OK;
+    if (b.p) {
+        cudaFree(b.p);
+        b.p = nullptr;
+        b.bytes = 0;
+    }
+    size_t want = bytes + bytes / 8;  // headroom for slowly growing chunks
+    cudaError_t e = cudaMalloc(&b.p, want);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        e = cudaMalloc(&b.p, bytes);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            b.p = nullptr;
+            return fail(ctx, DMANN_ERR_NOMEM,
+                        "device allocation of " + std::to_string(bytes) + " bytes failed");
+        }
+        want = bytes;
+    }
+    b.bytes = want;
+    return DMANN_OK;
+}
+
+bool is_device_ptr(const void *p) {
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
+}
+
+Hpx make_hpx(int nside) {
+    Hpx g;
+    g.nside = nside;
+    g.npix = 12 * nside * nside;
+    g.ncap = 2 * nside * (nside - 1);
+    g.nrings = 4 * nside - 1;
+    g.fact2 = 4.0 / (double)g.npix;
+    g.fact1 = (double)(nside << 1) * g.fact2;
+    g.dOmega = 4 * 3.14159265358979323846 / (double)g.npix;  // datatypes.h:251
+    g.theta0 = std::acos(1.0 - g.dOmega / (2.0 * 3.141592));   // genmap.cpp:38
+    return g;
+}
+
+// z, sin(theta) and theta of every ring, as pix2vec computes them for the
+// ring's pixels (sin(theta) from 1 - z near the poles).
+dmann_status ring_tables(dmann_ctx *ctx, int nside, RingTables &out) {
+    auto it = ctx->rings.find(nside);
+    if (it != ctx->rings.end()) {
+        out = it->second;
+        return DMANN_OK;
+    }
+    const Hpx g = make_hpx(nside);
+    const int n = 4 * nside;
+    std::vector<double> z(n, 0.0), st(n, 0.0), th(n, 0.0);
+    for (int r = 1; r < n; r++) {
+        bool have = false;
+        double tmp = 0.0;
+        if (r < nside) {
+            tmp = (double)((long long)r * r) * g.fact2;
+            z[r] = 1.0 - tmp;
+            have = z[r] > 0.99;
+        } else if (r <= 3 * nside) {
+            z[r] = (double)(2 * nside - r) * g.fact1;
+        } else {
+            long long ir = 4LL * nside - r;
+            tmp = (double)(ir * ir) * g.fact2;
+            z[r] = tmp - 1.0;
+            have = z[r] < -0.99;
+        }
+        st[r] = have ? std::sqrt(tmp * (2.0 - tmp)) : std::sqrt((1.0 - z[r]) * (1.0 + z[r]));
+        th[r] = have ? std::atan2(st[r], z[r]) : std::acos(z[r]);
+    }
+    RingTables t;
+    CK(cudaMalloc(&t.z, sizeof(double) * n));
+    CK(cudaMalloc(&t.st, sizeof(double) * n));
+    CK(cudaMalloc(&t.theta, sizeof(double) * n));
+    CK(cudaMemcpy(t.z, z.data(), sizeof(double) * n, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(t.st, st.data(), sizeof(double) * n, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(t.theta, th.data(), sizeof(double) * n, cudaMemcpyHostToDevice));
+    ctx->rings[nside] = t;
+    out = t;
+    return DMANN_OK;
+}
+
+dmann_status collect_stats(dmann_ctx *ctx) {
+    if (!ctx->stats_pending) return DMANN_OK;
+    CK(cudaStreamSynchronize(ctx->stream));
+    float ms = 0.0f;
+    CK(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
+    ctx->stats.kernel_ms = ms;
+    ctx->stats.disc_ms = 0.0;
+    if (ctx->disc_timed) {
+        CK(cudaEventElapsedTime(&ms, ctx->evd0, ctx->evd1));
+        ctx->stats.disc_ms = ms;
+    }
+    ctx->stats.n_kept = ctx->h_ctr[C_KEPT];
+    ctx->stats.n_invalid = ctx->h_ctr[C_INVALID];
+    ctx->stats.n_single = ctx->h_ctr[C_SINGLE];
+    ctx->stats.n_disc = ctx->h_ctr[C_DISC];
+    ctx->stats.n_disc_block = ctx->h_ctr[C_DISC_BLOCK];
+    ctx->stats.deposits = ctx->h_ctr[C_DEPOSITS];
+    ctx->stats.total_flux = *ctx->h_fsum;
+    ctx->stats_pending = false;
+    return DMANN_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int dmann_abi_version(void) { return DMANN_ABI_VERSION; }
+
+dmann_status dmann_create(dmann_ctx **out, int device) {
+    if (!out) return DMANN_ERR_INVALID;
+    *out = nullptr;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        return DMANN_ERR_NODEVICE;
+    }
+    if (device < 0 || device >= ndev) return DMANN_ERR_INVALID;
+    cudaDeviceProp prop;
+    if (cudaGetDeviceProperties(&prop, device) != cudaSuccess) return DMANN_ERR_CUDA;
+    if (!(prop.major == 10 && prop.minor == 3)) return DMANN_ERR_NODEVICE;  // built for sm_103a only
+    dmann_ctx *ctx = new dmann_ctx();
+    ctx->device = device;
+    ctx->num_sms = prop.multiProcessorCount;
+    if (cudaSetDevice(device) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&ctx->own, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreate(&ctx->ev0) != cudaSuccess || cudaEventCreate(&ctx->ev1) != cudaSuccess ||
+        cudaEventCreate(&ctx->evd0) != cudaSuccess || cudaEventCreate(&ctx->evd1) != cudaSuccess ||
+        cudaHostAlloc((void **)&ctx->h_ctr, 8 * (C_COUNT + 1), cudaHostAllocDefault) != cudaSuccess) {
+        cudaGetLastError();
+        delete ctx;
+        return DMANN_ERR_CUDA;
+    }
+    ctx->h_fsum = (double *)(ctx->h_ctr + C_COUNT);
+    ctx->stream = ctx->own;
+    ctx->tune.warp_max_pixels = 1024;
+    ctx->tune.block_threads = 256;
+    ctx->tune.blocks_per_sm = 0;
+    ctx->tune.ring_chunk = 256;
+    *out = ctx;
+    return DMANN_OK;
+}
+
+void dmann_destroy(dmann_ctx *ctx) {
+    if (!ctx) return;
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    DevBuf *bufs[] = {&ctx->in[0], &ctx->in[1], &ctx->in[2], &ctx->in[3], &ctx->in[4], &ctx->in[5],
+                      &ctx->theta, &ctx->phi, &ctx->ar, &ctx->flux, &ctx->cpix, &ctx->key,
+                      &ctx->queue, &ctx->hist, &ctx->ctr, &ctx->fsum, &ctx->acc, &ctx->map};
+    for (DevBuf *b : bufs)
+        if (b->p) cudaFree(b->p);
+    for (auto &kv : ctx->rings) {
+        cudaFree(kv.second.z);
+        cudaFree(kv.second.st);
+        cudaFree(kv.second.theta);
+    }
+    if (ctx->h_ctr) cudaFreeHost(ctx->h_ctr);
+    if (ctx->ev0) cudaEventDestroy(ctx->ev0);
+    if (ctx->evd0) cudaEventDestroy(ctx->evd0);
+    if (ctx->evd1) cudaEventDestroy(ctx->evd1);
+    if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+    if (ctx->own) cudaStreamDestroy(ctx->own);
+    delete ctx;
+}
+
+const char *dmann_last_error(const dmann_ctx *ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+dmann_status dmann_set_stream(dmann_ctx *ctx, void *stream) {
+    if (!ctx) return DMANN_ERR_INVALID;
+    ctx->stream = stream ? (cudaStream_t)stream : ctx->own;
+    return DMANN_OK;
+}
+
+dmann_status dmann_synchronize(dmann_ctx *ctx) {
+    if (!ctx) return DMANN_ERR_INVALID;
+    CK(cudaSetDevice(ctx->device));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return DMANN_OK;
+}
+
+dmann_status dmann_set_observer(dmann_ctx *ctx, const double opos[3], const double cpos[3],
+                                const double align[3]) {
+    if (!ctx || !opos || !cpos || !align) return fail(ctx, DMANN_ERR_INVALID, "null argument");
+    double rot[9];
+    if (!observer_rotation(opos, cpos, align, rot, nullptr, nullptr))
+        return fail(ctx, DMANN_ERR_INVALID, "observer position equals the halo centre");
+    std::memcpy(ctx->rot, rot, sizeof rot);
+    std::memcpy(ctx->opos, opos, sizeof(double) * 3);
+    ctx->have_frame = true;
+    return DMANN_OK;
+}
+
+dmann_status dmann_set_frame(dmann_ctx *ctx, const double rot[9], const double opos[3]) {
+    if (!ctx || !rot || !opos) return fail(ctx, DMANN_ERR_INVALID, "null argument");
+    for (int i = 0; i < 9; i++)
+        if (!std::isfinite(rot[i])) return fail(ctx, DMANN_ERR_INVALID, "non-finite rotation");
+    std::memcpy(ctx->rot, rot, sizeof(double) * 9);
+    std::memcpy(ctx->opos, opos, sizeof(double) * 3);
+    ctx->have_frame = true;
+    return DMANN_OK;
+}
+
+dmann_status dmann_set_units(dmann_ctx *ctx, double unit_factor, double hires_threshold,
+                             int flux_model) {
+    if (!ctx) return DMANN_ERR_INVALID;
+    if (!(std::isfinite(unit_factor) && unit_factor > 0))
+        return fail(ctx, DMANN_ERR_INVALID, "unit_factor must be finite and positive");
+    if (flux_model != DMANN_FLUX_ANN_NOSOM) return fail(ctx, DMANN_ERR_INVALID, "unknown flux model");
+    ctx->unit_factor = unit_factor;
+    ctx->hires = hires_threshold;
+    ctx->flux_model = flux_model;
+    ctx->have_units = true;
+    return DMANN_OK;
+}
+
+dmann_status dmann_set_tuning(dmann_ctx *ctx, const dmann_tuning *t) {
+    if (!ctx || !t) return DMANN_ERR_INVALID;
+    if (t->warp_max_pixels > 0) ctx->tune.warp_max_pixels = t->warp_max_pixels;
+    if (t->blocks_per_sm > 0) ctx->tune.blocks_per_sm = t->blocks_per_sm;
+    return DMANN_OK;
+}
+
+dmann_status dmann_get_tuning(const dmann_ctx *ctx, dmann_tuning *t) {
+    if (!ctx || !t) return DMANN_ERR_INVALID;
+    *t = ctx->tune;
+    return DMANN_OK;
+}
+
+dmann_status dmann_get_stats(const dmann_ctx *ctx_c, dmann_stats *out) {
+    dmann_ctx *ctx = const_cast<dmann_ctx *>(ctx_c);
+    if (!ctx || !out) return DMANN_ERR_INVALID;
+    CK(cudaSetDevice(ctx->device));
+    dmann_status s = collect_stats(ctx);
+    if (s != DMANN_OK) return s;
+    *out = ctx->stats;
+    return DMANN_OK;
+}
+
+namespace {
+
+dmann_status check_particles(dmann_ctx *ctx, const float *x, const float *y, const float *z,
+                             const float *m, const float *rho, const float *h, int64_t n) {
+    if (n < 0 || n > (int64_t)0x7fffffff)
+        return fail(ctx, DMANN_ERR_INVALID, "particle count out of range [0, 2^31)");
+    if (n > 0 && (!x || !y || !z || !m || !rho || !h))
+        return fail(ctx, DMANN_ERR_INVALID, "null particle array");
+    return DMANN_OK;
+}
+
+Frame make_frame(const dmann_ctx *ctx, double *scale) {
+    Frame f;
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) f.rot[i][j] = ctx->rot[3 * i + j];
+    for (int i = 0; i < 3; i++) f.opos[i] = ctx->opos[i];
+    f.unit_factor = ctx->unit_factor;
+    f.hires_threshold = ctx->hires;
+    int e2 = 0;
+    std::frexp(ctx->unit_factor, &e2);
+    f.inv_scale = std::ldexp(1.0, -e2);  // FP32 deposits hold flux / 2^e2 (exact scaling)
+    *scale = std::ldexp(1.0, e2);
+    f.flux_model = ctx->flux_model;
+    return f;
+}
+
+Accum make_accum(dmann_ctx *ctx) {
+    Accum acc;
+    const size_t P = (size_t)ctx->g.npix;
+    acc.acc64 = (double *)ctx->acc.p;
+    acc.hi = (float *)ctx->acc.p;
+    acc.lo = (float *)ctx->acc.p + P;
+    return acc;
+}
+
+}  // namespace
+
+dmann_status dmann_map_begin(dmann_ctx *ctx, int nside, int precision) {
+    if (!ctx) return DMANN_ERR_INVALID;
+    if (nside < 1 || nside > 8192) return fail(ctx, DMANN_ERR_INVALID, "nside must be in [1, 8192]");
+    if (precision != DMANN_PLAIN_F64 && precision != DMANN_COMP_F32)
+        return fail(ctx, DMANN_ERR_INVALID, "unknown precision form");
+    if (!ctx->have_frame) return fail(ctx, DMANN_ERR_STATE, "observer frame not set");
+    if (!ctx->have_units) return fail(ctx, DMANN_ERR_STATE, "units not set");
+    CK(cudaSetDevice(ctx->device));
+    dmann_status st = collect_stats(ctx);
+    if (st != DMANN_OK) return st;
+    ctx->g = make_hpx(nside);
+    ctx->precision = precision;
+    if ((st = ring_tables(ctx, nside, ctx->rt)) != DMANN_OK) return st;
+    const size_t P = (size_t)ctx->g.npix;
+    if ((st = ensure(ctx, ctx->acc, 8 * P)) || (st = ensure(ctx, ctx->hist, 4 * (size_t)kKeys)) ||
+        (st = ensure(ctx, ctx->ctr, 8 * C_COUNT)) || (st = ensure(ctx, ctx->fsum, 8)))
+        return st;
+    cudaStream_t s = ctx->stream;
+    CK(cudaEventRecord(ctx->ev0, s));
+    CK(cudaMemsetAsync(ctx->acc.p, 0, 8 * P, s));
+    CK(cudaMemsetAsync(ctx->ctr.p, 0, 8 * C_COUNT, s));
+    CK(cudaMemsetAsync(ctx->fsum.p, 0, 8, s));
+    ctx->stats = dmann_stats{};
+    ctx->disc_timed = false;
+    ctx->in_map = true;
+    return DMANN_OK;
+}
+
+dmann_status dmann_map_add(dmann_ctx *ctx, const float *x, const float *y, const float *z,
+                           const float *m, const float *rho, const float *h, int64_t n) {
+    if (!ctx) return DMANN_ERR_INVALID;
+    if (!ctx->in_map) return fail(ctx, DMANN_ERR_STATE, "dmann_map_add outside begin/end");
+    dmann_status st = check_particles(ctx, x, y, z, m, rho, h, n);
+    if (st != DMANN_OK) return st;
+    ctx->stats.n_in += n;
+    if (n == 0) return DMANN_OK;
+    CK(cudaSetDevice(ctx->device));
+    cudaStream_t s = ctx->stream;
+    const size_t N = (size_t)n;
+    if ((st = ensure(ctx, ctx->theta, 8 * N)) || (st = ensure(ctx, ctx->phi, 8 * N)) ||
+        (st = ensure(ctx, ctx->ar, 8 * N)) || (st = ensure(ctx, ctx->flux, 8 * N)) ||
+        (st = ensure(ctx, ctx->cpix, 4 * N)) || (st = ensure(ctx, ctx->key, 4 * N)) ||
+        (st = ensure(ctx, ctx->queue, 4 * N)))
+        return st;
+    // inputs: device pointers are used in place, host arrays are copied
+    const float *src[6] = {x, y, z, m, rho, h};
+    const float *dev[6];
+    for (int k = 0; k < 6; k++) {
+        if (is_device_ptr(src[k])) {
+            dev[k] = src[k];
+        } else {
+            if ((st = ensure(ctx, ctx->in[k], 4 * N)) != DMANN_OK) return st;
+            CK(cudaMemcpyAsync(ctx->in[k].p, src[k], 4 * N, cudaMemcpyHostToDevice, s));
+            dev[k] = (const float *)ctx->in[k].p;
+        }
+    }
+    double scale;
+    const Frame f = make_frame(ctx, &scale);
+    const Accum acc = make_accum(ctx);
+    int bmin = 0;
+    while (bmin < kBuckets && (1LL << bmin) <= ctx->tune.warp_max_pixels) bmin++;
+
+    CK(cudaMemsetAsync(ctx->hist.p, 0, 4 * (size_t)kKeys, s));
+    CK(cudaMemsetAsync((long long *)ctx->ctr.p + kCtrChunkFirst, 0, 8 * (C_COUNT - kCtrChunkFirst), s));
+    PrepArgs pa;
+    pa.p = {dev[0], dev[1], dev[2], dev[3], dev[4], dev[5], (int)N};
+    pa.f = f;
+    pa.g = ctx->g;
+    pa.out = {(double *)ctx->theta.p, (double *)ctx->phi.p, (double *)ctx->ar.p,
+              (double *)ctx->flux.p, (int *)ctx->cpix.p, (int *)ctx->key.p};
+    pa.hist = (int *)ctx->hist.p;
+    pa.ctr = (long long *)ctx->ctr.p;
+    pa.flux_sum = (double *)ctx->fsum.p;
+    pa.acc = acc;
+    pa.precision = ctx->precision;
+    pa.block_bucket_min = bmin;
+    CK(launch_prep(pa, s));
+    CK(launch_scan(pa.hist, pa.ctr, bmin, s));
+    CK(launch_scatter(pa, (int *)ctx->queue.p, s));
+
+    DiscArgs da;
+    da.g = ctx->g;
+    da.f = f;
+    da.rt = {ctx->rt.z, ctx->rt.st, ctx->rt.theta};
+    da.theta = pa.out.theta;
+    da.phi = pa.out.phi;
+    da.ar = pa.out.ar;
+    da.flux = pa.out.flux;
+    da.cpix = pa.out.cpix;
+    da.queue = (const int *)ctx->queue.p;
+    da.ctr = pa.ctr;
+    da.acc = acc;
+    CK(cudaEventRecord(ctx->evd0, s));
+    if (ctx->precision == DMANN_PLAIN_F64) CK(launch_disc_plain(da, ctx->num_sms, ctx->tune.blocks_per_sm, s));
+    else CK(launch_disc_comp(da, ctx->num_sms, ctx->tune.blocks_per_sm, s));
+    CK(cudaEventRecord(ctx->evd1, s));
+    ctx->disc_timed = true;
+    return DMANN_OK;
+}
+
+dmann_status dmann_map_end(dmann_ctx *ctx, double *map_out, int accumulate) {
+    if (!ctx) return DMANN_ERR_INVALID;
+    if (!ctx->in_map) return fail(ctx, DMANN_ERR_STATE, "dmann_map_end without dmann_map_begin");
+    if (!map_out) return fail(ctx, DMANN_ERR_INVALID, "map_out is null");
+    CK(cudaSetDevice(ctx->device));
+    cudaStream_t s = ctx->stream;
+    const size_t P = (size_t)ctx->g.npix;
+    dmann_status st;
+    const bool map_dev = is_device_ptr(map_out);
+    double *dmap = map_out;
+    if (!map_dev) {
+        if ((st = ensure(ctx, ctx->map, 8 * P)) != DMANN_OK) return st;
+        dmap = (double *)ctx->map.p;
+        if (accumulate) CK(cudaMemcpyAsync(dmap, map_out, 8 * P, cudaMemcpyHostToDevice, s));
+    }
+    double scale;
+    (void)make_frame(ctx, &scale);
+    CK(launch_finalize(make_accum(ctx), ctx->precision, ctx->g.npix, ctx->g.dOmega, scale, dmap,
+                       accumulate, s));
+    CK(cudaEventRecord(ctx->ev1, s));
+    CK(cudaMemcpyAsync(ctx->h_ctr, ctx->ctr.p, 8 * C_COUNT, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(ctx->h_fsum, ctx->fsum.p, 8, cudaMemcpyDeviceToHost, s));
+    ctx->stats_pending = true;
+    ctx->in_map = false;
+    if (!map_dev) {
+        CK(cudaMemcpyAsync(map_out, dmap, 8 * P, cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+    }
+    return DMANN_OK;
+}
+
+dmann_status dmann_render(dmann_ctx *ctx, const float *x, const float *y, const float *z,
+                          const float *m, const float *rho, const float *h, int64_t n, int nside,
+                          int precision, double *map_out, int accumulate) {
+    if (!ctx) return DMANN_ERR_INVALID;
+    if (!map_out) return fail(ctx, DMANN_ERR_INVALID, "map_out is null");
+    dmann_status st = check_particles(ctx, x, y, z, m, rho, h, n);
+    if (st != DMANN_OK) return st;
+    if ((st = dmann_map_begin(ctx, nside, precision)) != DMANN_OK) return st;
+    if ((st = dmann_map_add(ctx, x, y, z, m, rho, h, n)) != DMANN_OK) {
+        ctx->in_map = false;
+        return st;
+    }
+    return dmann_map_end(ctx, map_out, accumulate);
+}
+
+dmann_status dmann_observer_rotation(const double opos[3], const double cpos[3],
+                                     const double align[3], double rot[9], double angles[2]) {
+    if (!opos || !cpos || !align || !rot) return DMANN_ERR_INVALID;
+    double th = 0, ph = 0;
+    if (!observer_rotation(opos, cpos, align, rot, &th, &ph)) return DMANN_ERR_INVALID;
+    if (angles) {
+        angles[0] = th;
+        angles[1] = ph;
+    }
+    return DMANN_OK;
+}
+
+dmann_status dmann_code_units(double h100, double Lbox_in_Mpc, double mass_to_Msun, double out[9]) {
+    if (!out) return DMANN_ERR_INVALID;
+    CodeUnits u;
+    setup_units(h100, Lbox_in_Mpc, mass_to_Msun, &u);
+    out[0] = u.rho_crit_in_cgs;
+    out[1] = u.length_to_cgs;
+    out[2] = u.time_to_cgs;
+    out[3] = u.density_to_cgs;
+    out[4] = u.mass_to_cgs;
+    out[5] = u.mass_to_Msun;
+    out[6] = u.velocity_to_cgs;
+    out[7] = u.annihilation_flux_to_cgs;
+    out[8] = nosom_unit_factor(u);
+    return DMANN_OK;
+}
+
+double dmann_hires_threshold(const double *masses, int n) {
+    return hires_threshold(masses, masses ? n : 0);
+}
+
+}  // extern "C"

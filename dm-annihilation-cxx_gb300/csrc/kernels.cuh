@@ -1,0 +1,80 @@
+// kernels.cuh -- argument blocks and launch entry points of the projection
+// kernels (prep.cu, disc_plain.cu, disc_comp.cu).  Host-callable wrappers
+// only take plain pointers and PODs.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+#include "common.cuh"
+
+namespace dmann {
+
+// Sort keys of disc particles: (31 - log2 size bucket) * kCells + sky cell,
+// so the queue runs from the largest discs to the smallest (longest jobs
+// first) and, within a size bucket, in sky order (neighbouring discs are
+// rendered together and share L2 lines of the map).
+constexpr int kCellBits = 12;
+constexpr int kCells = 1 << kCellBits;
+constexpr int kBuckets = 32;
+constexpr int kKeys = kBuckets * kCells;
+
+// Device counters (int64).  The first six accumulate over every chunk of
+// a map; the C_ADD_* ones describe the chunk being added and are reset for
+// each chunk.
+enum Ctr {
+    C_KEPT = 0, C_SINGLE, C_DISC, C_DISC_BLOCK, C_DEPOSITS, C_INVALID,
+    C_ADD_DISC, C_ADD_BLOCK, C_QNEXT_BLOCK, C_QNEXT_WARP, C_COUNT
+};
+constexpr int kCtrChunkFirst = C_ADD_DISC;
+
+struct Particles {
+    const float *x, *y, *z, *m, *rho, *h;
+    int n;
+};
+
+// Per-particle geometry written by the prep kernel (FP64).
+struct PrepOut {
+    double *theta, *phi, *ar, *flux;
+    int *cpix;
+    int *key;     // sort key, -1 for skipped / single-pixel particles
+};
+
+struct Accum {
+    double *acc64;      // DMANN_PLAIN_F64
+    float *hi, *lo;     // DMANN_COMP_F32 (compensated two-float planes)
+};
+
+struct PrepArgs {
+    Particles p;
+    Frame f;
+    Hpx g;
+    PrepOut out;
+    int *hist;                  // [kKeys]
+    long long *ctr;             // [C_COUNT]
+    double *flux_sum;           // [1] total kept flux
+    Accum acc;
+    int precision;
+    int block_bucket_min;       // discs whose size bucket >= this go block-per-particle
+};
+
+struct DiscArgs {
+    Hpx g;
+    Frame f;
+    RingTab rt;
+    const double *theta, *phi, *ar, *flux;
+    const int *cpix;
+    const int *queue;           // disc particles, largest first
+    long long *ctr;
+    Accum acc;
+};
+
+// prep.cu
+cudaError_t launch_prep(const PrepArgs &a, cudaStream_t s);
+cudaError_t launch_scan(int *hist, long long *ctr, int block_bucket_min, cudaStream_t s);
+cudaError_t launch_scatter(const PrepArgs &a, int *queue, cudaStream_t s);
+cudaError_t launch_finalize(const Accum &acc, int precision, int npix, double dOmega,
+                            double scale, double *out, int accumulate, cudaStream_t s);
+// disc_plain.cu / disc_comp.cu
+cudaError_t launch_disc_plain(const DiscArgs &a, int num_sms, int blocks_per_sm, cudaStream_t s);
+cudaError_t launch_disc_comp(const DiscArgs &a, int num_sms, int blocks_per_sm, cudaStream_t s);
+
+}  // namespace dmann

@@ -1,0 +1,93 @@
+"""ctypes binding of libdmann.so (the C ABI declared in include/dmann.h).
+
+The library is the only compute path: if it is missing or fails to load
+this module raises, and there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import threading
+
+PKG_DIR = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+LIB_PATH = os.path.join(PKG_DIR, "libdmann.so")
+
+OK, ERR_INVALID, ERR_CUDA, ERR_NOMEM, ERR_STATE, ERR_TIMEOUT, ERR_NODEVICE = range(7)
+STATUS_NAMES = {0: "OK", 1: "INVALID", 2: "CUDA", 3: "NOMEM", 4: "STATE", 5: "TIMEOUT", 6: "NODEVICE"}
+PLAIN_F64, COMP_F32 = 0, 1
+FLUX_ANN_NOSOM = 0
+
+
+class DmannError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__(f"dmann status {STATUS_NAMES.get(status, status)}: {msg}")
+        self.status = status
+
+
+class Stats(C.Structure):
+    _fields_ = [("n_in", C.c_int64), ("n_kept", C.c_int64), ("n_invalid", C.c_int64),
+                ("n_single", C.c_int64),
+                ("n_disc", C.c_int64), ("n_disc_block", C.c_int64), ("deposits", C.c_int64),
+                ("kernel_ms", C.c_double), ("disc_ms", C.c_double),
+                ("total_flux", C.c_double)]
+
+
+class Tuning(C.Structure):
+    _fields_ = [("warp_max_pixels", C.c_int64), ("block_threads", C.c_int32),
+                ("blocks_per_sm", C.c_int32), ("ring_chunk", C.c_int32),
+                ("reserved", C.c_int32 * 3)]
+
+
+_LIB = None
+_LOCK = threading.Lock()
+
+# name -> (restype, argtypes)
+_P = C.c_void_p
+_D3 = C.POINTER(C.c_double)
+_F = C.POINTER(C.c_float)
+SIGNATURES = {
+    "dmann_abi_version": (C.c_int, []),
+    "dmann_create": (C.c_int, [C.POINTER(_P), C.c_int]),
+    "dmann_destroy": (None, [_P]),
+    "dmann_last_error": (C.c_char_p, [_P]),
+    "dmann_set_stream": (C.c_int, [_P, _P]),
+    "dmann_synchronize": (C.c_int, [_P]),
+    "dmann_set_observer": (C.c_int, [_P, _D3, _D3, _D3]),
+    "dmann_set_frame": (C.c_int, [_P, _D3, _D3]),
+    "dmann_set_units": (C.c_int, [_P, C.c_double, C.c_double, C.c_int]),
+    "dmann_set_tuning": (C.c_int, [_P, C.POINTER(Tuning)]),
+    "dmann_get_tuning": (C.c_int, [_P, C.POINTER(Tuning)]),
+    "dmann_render": (C.c_int, [_P, _P, _P, _P, _P, _P, _P, C.c_int64, C.c_int, C.c_int, _P, C.c_int]),
+    "dmann_map_begin": (C.c_int, [_P, C.c_int, C.c_int]),
+    "dmann_map_add": (C.c_int, [_P, _P, _P, _P, _P, _P, _P, C.c_int64]),
+    "dmann_map_end": (C.c_int, [_P, _P, C.c_int]),
+    "dmann_get_stats": (C.c_int, [_P, C.POINTER(Stats)]),
+    "dmann_observer_rotation": (C.c_int, [_D3, _D3, _D3, _D3, _D3]),
+    "dmann_code_units": (C.c_int, [C.c_double, C.c_double, C.c_double, _D3]),
+    "dmann_hires_threshold": (C.c_double, [_D3, C.c_int]),
+}
+
+
+def load(path: str = LIB_PATH):
+    """Loads libdmann.so (building it in-tree first if it is absent)."""
+    global _LIB
+    with _LOCK:
+        if _LIB is not None:
+            return _LIB
+        if not os.path.exists(path):
+            import importlib.util
+            spec = importlib.util.spec_from_file_location("_dmann_build", os.path.join(PKG_DIR, "build.py"))
+            mod = importlib.util.module_from_spec(spec)
+            spec.loader.exec_module(mod)
+            mod.build()
+        lib = C.CDLL(path)
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(lib, name)
+            fn.restype = res
+            fn.argtypes = args
+        _LIB = lib
+        return lib
+
+
+def exported_symbols():
+    return list(SIGNATURES)

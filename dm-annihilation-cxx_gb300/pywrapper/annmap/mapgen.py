@@ -1,0 +1,208 @@
+"""Renderer (a handle on the native library) and MapGenerator (the reference's
+map-generator API, src/mapgenerator.h:8-26, on top of it).
+
+``MapGenerator(par, reader).start()`` streams the reader's chunks through
+dmann_map_begin / dmann_map_add / dmann_map_end exactly where the reference's
+start() loops over DataReader chunks (src/genmap.cpp:67-156); ``getMap()``
+returns the FP64 RING map in flux per steradian (after the dOmega division,
+genmap.cpp:168), ``getNside()`` and ``isFinished()`` as in the reference.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib
+from ._lib import COMP_F32, PLAIN_F64, DmannError
+
+FIELDS = ("x", "y", "z", "m", "rho", "h")
+
+
+def _is_torch(a):
+    return type(a).__module__.startswith("torch")
+
+
+class Renderer:
+    """One native context (its own CUDA stream and device workspace)."""
+
+    def __init__(self, device: int = 0):
+        self.L = _lib.load()
+        self.ctx = C.c_void_p()
+        st = self.L.dmann_create(C.byref(self.ctx), int(device))
+        if st != _lib.OK:
+            raise DmannError(st, "dmann_create failed (a GB300 / sm_103 device is required)")
+        self.device = device
+        self._keep = []
+        self._nside = None
+
+    # ------------------------------------------------------------ plumbing
+    def _check(self, st):
+        if st != _lib.OK:
+            msg = self.L.dmann_last_error(self.ctx)
+            raise DmannError(st, msg.decode() if msg else "")
+
+    def close(self):
+        if self.ctx:
+            self.L.dmann_destroy(self.ctx)
+            self.ctx = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def _ptr(self, a, dtype):
+        """Raw pointer of a contiguous numpy array or torch tensor (kept alive)."""
+        if _is_torch(a):
+            import torch
+            want = torch.float32 if dtype == np.float32 else torch.float64
+            if a.dtype != want or not a.is_contiguous():
+                a = a.to(want).contiguous()
+            self._keep.append(a)
+            return C.c_void_p(a.data_ptr())
+        arr = np.ascontiguousarray(a, dtype=dtype)
+        self._keep.append(arr)
+        return C.c_void_p(arr.ctypes.data)
+
+    def set_stream(self, stream=None):
+        """Runs on a cudaStream_t (an int handle or a torch.cuda.Stream)."""
+        h = getattr(stream, "cuda_stream", stream)
+        self._check(self.L.dmann_set_stream(self.ctx, C.c_void_p(h) if h else None))
+
+    def _use_torch_stream(self, arrays):
+        if any(_is_torch(a) and a.is_cuda for a in arrays):
+            import torch
+            self.set_stream(torch.cuda.current_stream(self.device))
+
+    # ------------------------------------------------------------ frame / units
+    def set_observer(self, opos, cpos, align):
+        d3 = lambda v: (C.c_double * 3)(*[float(x) for x in v])
+        self._check(self.L.dmann_set_observer(self.ctx, d3(opos), d3(cpos), d3(align)))
+
+    def set_frame(self, rot, opos):
+        r = np.asarray(rot, dtype=np.float64).reshape(9)
+        self._check(self.L.dmann_set_frame(self.ctx, (C.c_double * 9)(*r.tolist()),
+                                           (C.c_double * 3)(*[float(x) for x in opos])))
+
+    def set_units(self, unit_factor: float, hires_threshold: float = float("inf"), flux_model: int = 0):
+        self._check(self.L.dmann_set_units(self.ctx, float(unit_factor), float(hires_threshold),
+                                           int(flux_model)))
+
+    def set_params(self, par):
+        """Frame and units from a Parameters object."""
+        self.set_frame(par.rotmatrix, par.params.opos)
+        self.set_units(par.unit_factor, par.hires_threshold)
+
+    def set_tuning(self, **kw):
+        t = _lib.Tuning()
+        for k, v in kw.items():
+            setattr(t, k, v)
+        self._check(self.L.dmann_set_tuning(self.ctx, C.byref(t)))
+
+    def get_tuning(self) -> dict:
+        t = _lib.Tuning()
+        self._check(self.L.dmann_get_tuning(self.ctx, C.byref(t)))
+        return {k: getattr(t, k) for k, _ in _lib.Tuning._fields_ if k != "reserved"}
+
+    # ------------------------------------------------------------ rendering
+    def begin(self, nside: int, precision: int = COMP_F32):
+        self._keep = []
+        self._nside = int(nside)
+        self._check(self.L.dmann_map_begin(self.ctx, int(nside), int(precision)))
+
+    def add(self, parts: dict):
+        arrays = [parts[k] for k in FIELDS]
+        n = len(arrays[0])
+        if any(len(a) != n for a in arrays):
+            raise ValueError("particle arrays differ in length")
+        self._use_torch_stream(arrays)
+        ptrs = [self._ptr(a, np.float32) for a in arrays]
+        self._check(self.L.dmann_map_add(self.ctx, *ptrs, int(n)))
+
+    def end(self, out=None, accumulate: bool = False):
+        npix = 12 * self._nside * self._nside
+        if out is None:
+            out = np.zeros(npix, dtype=np.float64)
+        if len(out) != npix:
+            raise ValueError("output map has the wrong length")
+        if _is_torch(out):
+            if out.dtype.is_floating_point and out.dtype.itemsize != 8 or not out.is_contiguous():
+                raise ValueError("output map must be a contiguous float64 tensor")
+            if out.is_cuda:
+                self._use_torch_stream([out])
+            ptr = C.c_void_p(out.data_ptr())
+        else:
+            if out.dtype != np.float64 or not out.flags.c_contiguous:
+                raise ValueError("output map must be a contiguous float64 array")
+            ptr = C.c_void_p(out.ctypes.data)
+        self._check(self.L.dmann_map_end(self.ctx, ptr, int(bool(accumulate))))
+        if not (_is_torch(out) and out.is_cuda):
+            self._keep = []
+        return out
+
+    def render(self, parts: dict, nside: int, precision: int = COMP_F32, out=None,
+               accumulate: bool = False):
+        self.begin(nside, precision)
+        self.add(parts)
+        return self.end(out, accumulate)
+
+    def synchronize(self):
+        self._check(self.L.dmann_synchronize(self.ctx))
+        self._keep = []
+
+    def stats(self) -> dict:
+        s = _lib.Stats()
+        self._check(self.L.dmann_get_stats(self.ctx, C.byref(s)))
+        return {k: getattr(s, k) for k, _ in _lib.Stats._fields_}
+
+
+class MapGenerator:
+    """The reference's MapGenerator (src/mapgenerator.h:8-26) on the GPU."""
+
+    def __init__(self, par, reader, precision: int = COMP_F32, device: int = 0):
+        self.par_ = par
+        self.reader_ = reader
+        self.precision = precision
+        self.device = device
+        self.map_ = None
+        self.isFinished_ = False
+        self.total_flux = None
+
+    def start(self):
+        r = Renderer(self.device)
+        try:
+            r.set_params(self.par_)
+            r.begin(self.par_.map.Nside, self.precision)
+            while self.reader_.hasNext():
+                r.add(self.reader_.next_chunk())
+            self.map_ = r.end()
+            st = r.stats()
+            self.total_flux = st["total_flux"]  # the reference's "Total Conts"
+            self.stats = st
+        finally:
+            r.close()
+        self.isFinished_ = True
+
+    def isFinished(self) -> bool:
+        return self.isFinished_
+
+    def getMap(self):
+        return self.map_
+
+    def getNside(self) -> int:
+        return self.par_.map.Nside
+
+    def saveToFits(self, fits_file: str, isVerbose: bool = False):
+        from .fitsio import write_healpix_map
+        if not self.isFinished():
+            print("Map not generated yet")
+            return
+        write_healpix_map(fits_file or self.par_.outputFileName, self.map_)

@@ -1,0 +1,182 @@
+/*
+ * dmann.h -- C ABI of the GB300 annihilation sky-map projection library
+ * (libdmann.so).
+ *
+ * Plain C types only: no C++ or torch types cross this boundary.  Every entry
+ * point returns a status code (never exits, never throws); the message of the
+ * last failure on a context is available from dmann_last_error().  Buffers
+ * are owned by the caller; a context owns only its stream and its device
+ * workspace.  One context per host thread / stream: calls on one context are
+ * serialised on its stream, different contexts are independent (reentrant).
+ *
+ * What each entry point replaces in the reference (paths relative to the
+ * reference project):
+ *   dmann_create / dmann_destroy      initializeCUDA / cudaCleaingUp
+ *                                     (src/chealpixrender.h:60-64,
+ *                                     src/kernel.h:10-11), which keep module-
+ *                                     global device state; here it is a handle.
+ *   dmann_set_observer                Parameters::setupParams / setupRotation
+ *                                     (src/parameters.cpp:111-152,183-289)
+ *   dmann_set_frame                   the rotmatrix/opos fields those set
+ *                                     (src/parameters.h:17, datatypes.h:225)
+ *   dmann_set_units                   getflux's unit factor and the hires-mass
+ *                                     filter (src/flux/flux_ann_nosom.cpp:13-16,
+ *                                     src/genmap.cpp:52-58,82-85)
+ *   dmann_render                      MapGenerator::start's per-chunk work:
+ *                                     the host prep loop plus
+ *                                     calculateMapByGPU / getCUDAMap
+ *                                     (src/genmap_cuda_render.cpp:102-196,
+ *                                     src/chealpixrender.h:61-63) and
+ *                                     calulateMapWithCUDA (src/kernel.h:11),
+ *                                     with the CPU semantics of
+ *                                     src/genmap.cpp:67-169.
+ *   dmann_render_batch                no reference counterpart (many
+ *                                     observers / Nside values in one call)
+ *   dmann_adjoint                     no reference counterpart (gradients of a
+ *                                     pixelwise loss)
+ */
+#ifndef DMANN_H
+#define DMANN_H
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define DMANN_ABI_VERSION 1
+
+typedef struct dmann_ctx dmann_ctx;
+
+typedef enum {
+    DMANN_OK = 0,
+    DMANN_ERR_INVALID = 1,   /* bad argument (null pointer, bad Nside, ...) */
+    DMANN_ERR_CUDA = 2,      /* a CUDA runtime call failed */
+    DMANN_ERR_NOMEM = 3,     /* device or host allocation failed */
+    DMANN_ERR_STATE = 4,     /* call order (e.g. render before an observer) */
+    DMANN_ERR_TIMEOUT = 5,   /* a bounded device wait gave up */
+    DMANN_ERR_NODEVICE = 6   /* no CUDA device / wrong architecture */
+} dmann_status;
+
+/* Precision forms of the projection. */
+typedef enum {
+    /* FP64 throughout: geometry, weights exp(-0.5 (acos(v_p.v)/ar)^2/0.333),
+     * normalisation and FP64 atomic accumulation -- the reference CPU path's
+     * arithmetic on the GPU. */
+    DMANN_PLAIN_F64 = 0,
+    /* FP64 per-particle geometry and disc bounds; FP32 weights (haversine
+     * distance, Gaussian); per-particle normalisation and per-pixel
+     * accumulation as compensated two-float (hi + lo) sums; FP64 final
+     * reduction.  The fast form. */
+    DMANN_COMP_F32 = 1
+} dmann_precision;
+
+/* Flux laws (the reference's link-time getflux plugins, src/flux/). */
+typedef enum {
+    DMANN_FLUX_ANN_NOSOM = 0   /* unit_factor * rho * m / (4 pi d^2) */
+} dmann_flux;
+
+/* Counters of the last dmann_render call on a context. */
+typedef struct {
+    int64_t n_in;          /* particles passed in */
+    int64_t n_kept;        /* passed the hires-mass and mask filter */
+    int64_t n_invalid;     /* skipped: at the observer or non-finite geometry */
+    int64_t n_single;      /* deposited into one pixel (2 ar < theta0) */
+    int64_t n_disc;        /* rendered as discs (incl. < 2 pixel discs) */
+    int64_t n_disc_block;  /* of which in the block-per-particle class */
+    int64_t deposits;      /* algorithmic deposits: sum of disc sizes + singles */
+    double kernel_ms;      /* device time from map_begin to map_end (events) */
+    double disc_ms;        /* device time of the disc kernels of the last chunk */
+    double total_flux;     /* sum of kept flux (before the dOmega division) */
+} dmann_stats;
+
+/* Tunables (an autotuner may set them; zero fields keep defaults). */
+typedef struct {
+    int64_t warp_max_pixels;   /* discs up to this estimate go warp-per-particle */
+    int32_t block_threads;     /* threads of the block-per-particle kernel */
+    int32_t blocks_per_sm;     /* resident blocks per SM for persistent kernels */
+    int32_t ring_chunk;        /* rings staged in shared memory per pass */
+    int32_t reserved[3];
+} dmann_tuning;
+
+/* ---- lifetime ---- */
+dmann_status dmann_create(dmann_ctx **ctx, int device);
+void dmann_destroy(dmann_ctx *ctx);
+const char *dmann_last_error(const dmann_ctx *ctx);
+int dmann_abi_version(void);
+
+/* Runs subsequent work on `stream` (a cudaStream_t; NULL = the context's
+ * own stream).  Lets a caller such as PyTorch share its current stream. */
+dmann_status dmann_set_stream(dmann_ctx *ctx, void *stream);
+dmann_status dmann_synchronize(dmann_ctx *ctx);
+
+/* ---- observer frame and units ---- */
+/* Observer at opos, halo centre cpos, alignment vector align: computes the
+ * rotation matrix exactly as Parameters::setupRotation does.  Fails with
+ * DMANN_ERR_INVALID when opos == cpos (the reference's angles are NaN). */
+dmann_status dmann_set_observer(dmann_ctx *ctx, const double opos[3],
+                                const double cpos[3], const double align[3]);
+/* Sets the frame directly: rot is rotmatrix[3][3] row-major, as used by
+ * calc_angles (v' = rot^T (pos - opos)). */
+dmann_status dmann_set_frame(dmann_ctx *ctx, const double rot[9],
+                             const double opos[3]);
+/* unit_factor multiplies rho*m/(4 pi d^2); hires_threshold is the mass at or
+ * above which a particle is skipped ((double)(float)min_mass * 1.1 in the
+ * reference; pass INFINITY to keep every particle). */
+dmann_status dmann_set_units(dmann_ctx *ctx, double unit_factor,
+                             double hires_threshold, int flux_model);
+dmann_status dmann_set_tuning(dmann_ctx *ctx, const dmann_tuning *t);
+dmann_status dmann_get_tuning(const dmann_ctx *ctx, dmann_tuning *t);
+
+/* ---- rendering ---- */
+/* Projects n particles (float32 SoA: positions x,y,z, mass m, density rho,
+ * smoothing length h; rho < 0 marks a masked particle) into a HEALPix RING
+ * map of 12*nside^2 doubles in flux per steradian (the reference's map after
+ * its final division by dOmega).  Inputs and map_out may each be host or
+ * device pointers (detected).  accumulate != 0 adds into map_out instead of
+ * overwriting it, so chunks of a particle stream can be rendered one call at
+ * a time.  1 <= nside <= 8192.  Blocks until map_out is complete when it is a
+ * host pointer; otherwise returns with the work queued on the stream. */
+dmann_status dmann_render(dmann_ctx *ctx, const float *x, const float *y,
+                          const float *z, const float *m, const float *rho,
+                          const float *h, int64_t n, int nside, int precision,
+                          double *map_out, int accumulate);
+
+/* Streaming form of dmann_render, the shape of MapGenerator::start's loop
+ * over DataReader chunks (src/genmap.cpp:67-156): begin zeroes the
+ * context's device accumulation planes for one map, every add deposits one
+ * chunk of particles into them (inputs host or device), end divides by
+ * dOmega into map_out (host or device; accumulate != 0 adds to it).  The
+ * compensated planes carry the sum across chunks, so a streamed map equals
+ * a single-call one to accumulation rounding. */
+dmann_status dmann_map_begin(dmann_ctx *ctx, int nside, int precision);
+dmann_status dmann_map_add(dmann_ctx *ctx, const float *x, const float *y,
+                           const float *z, const float *m, const float *rho,
+                           const float *h, int64_t n);
+dmann_status dmann_map_end(dmann_ctx *ctx, double *map_out, int accumulate);
+
+/* Statistics of the last completed map (synchronises the stream). */
+dmann_status dmann_get_stats(const dmann_ctx *ctx, dmann_stats *out);
+
+/* ---- host-only helpers (no context, no GPU) ---- */
+/* Parameters::setupParams + setupRotation (src/parameters.cpp:111-152,
+ * 183-289): rot = rotmatrix row-major; angles = {otheta, ophi} (may be
+ * NULL).  DMANN_ERR_INVALID when opos == cpos. */
+dmann_status dmann_observer_rotation(const double opos[3], const double cpos[3],
+                                     const double align[3], double rot[9],
+                                     double angles[2]);
+/* Parameters::setupUnits (src/parameters.cpp:42-82) and the default flux
+ * law's unit factor (src/flux/flux_ann_nosom.cpp:13-16).  out = {rho_crit,
+ * length_to_cgs, time_to_cgs, density_to_cgs, mass_to_cgs, mass_to_Msun,
+ * velocity_to_cgs, annihilation_flux_to_cgs, unit_factor}.  mass_to_Msun
+ * = -1 derives the mass unit from rho_crit * L^3, as the reference does. */
+dmann_status dmann_code_units(double h100, double Lbox_in_Mpc,
+                              double mass_to_Msun, double out[9]);
+/* src/genmap.cpp:52-58: (double)(float)min(masses > 0) * 1.1, the mass at
+ * or above which a particle is skipped (FLT_MAX * 1.1 if none positive). */
+double dmann_hires_threshold(const double *masses, int n);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* DMANN_H */

@@ -1,0 +1,222 @@
+"""GPU parity: the CUDA projection (through the C ABI) against the reference.
+
+  * golden fixtures -- maps made by the reference's own genmap.cpp build;
+  * the FP64 oracle on larger seeded synthetic halos;
+  * size-independent properties at full Nside: flux conservation
+    (sum(map) * dOmega == sum of kept flux, the reference's "Total Conts"),
+    linearity (chunked streaming == one call, accumulate doubles the map),
+    host and device inputs agree.
+
+Tolerances (stated per the contract of the two forms):
+  plain FP64   per-pixel relative error <= 1e-10 (only the order of the FP64
+               additions differs from the CPU path); total flux 1e-12
+  compensated  per-pixel relative error: median <= 1e-5, max <= 1e-4; total
+               flux <= 1e-9
+  Relative errors are taken over pixels whose reference value exceeds
+  1e-6 of the map maximum; the set of non-zero pixels must match exactly
+  (disc membership is decided in FP64 by both forms).
+"""
+import math
+
+import numpy as np
+import pytest
+
+import annmap
+import golden_cases as G
+import oracle as O
+from annmap import synth
+
+pytestmark = pytest.mark.gpu
+
+PLAIN, COMP = annmap.PLAIN_F64, annmap.COMP_F32
+FLOOR = 1e-6
+
+
+def rel_errors(got, ref):
+    mask = ref > FLOOR * ref.max()
+    rel = np.abs(got[mask] - ref[mask]) / ref[mask]
+    return float(np.median(rel)), float(rel.max())
+
+
+def check(got, ref, precision, total=None, dOmega=None):
+    assert np.all(np.isfinite(got))
+    assert np.array_equal(got != 0, ref != 0), "non-zero pixel sets differ"
+    med, mx = rel_errors(got, ref)
+    if precision == PLAIN:
+        assert mx <= 1e-10, (med, mx)
+    else:
+        assert med <= 1e-5 and mx <= 1e-4, (med, mx)
+    if total is not None:
+        tol = 1e-12 if precision == PLAIN else 1e-9
+        assert math.isclose(got.sum() * dOmega, total, rel_tol=tol), (got.sum() * dOmega, total)
+    return med, mx
+
+
+@pytest.fixture(scope="module")
+def rend():
+    r = annmap.Renderer(0)
+    yield r
+    r.close()
+
+
+@pytest.mark.parametrize("precision", [PLAIN, COMP])
+@pytest.mark.parametrize("name", G.names())
+def test_golden_maps(rend, name, precision):
+    case = G.load(name)
+    p = annmap.Parameters(text=case["info_text"].replace("@DIR@", "/x"))
+    rend.set_params(p)
+    got = rend.render(case["parts"], p.map.Nside, precision)
+    ref = case["map"]
+    st = rend.stats()
+    check(got, ref, precision, total=ref.sum() * p.map.dOmega, dOmega=p.map.dOmega)
+    assert math.isclose(st["total_flux"], ref.sum() * p.map.dOmega, rel_tol=1e-12)
+
+
+@pytest.mark.parametrize("precision", [PLAIN, COMP])
+def test_golden_via_mapgenerator(tmp_path, precision):
+    """The reference's own flow: info file + native data file (+ mask, test
+    limit, chunked buffer) through MapGenerator."""
+    case = G.load("hires_mask_ns32")
+    z = np.load(G.GOLDEN + "/hires_mask_ns32.npz")
+    rec, mask = z["records"], z["mask"]
+    data = tmp_path / "parts.bin"
+    with open(data, "wb") as f:
+        np.array([len(rec)], np.int32).tofile(f)
+        rec.tofile(f)
+    mpath = tmp_path / "mask.bin"
+    with open(mpath, "wb") as f:
+        np.array([len(rec)], np.int32).tofile(f)
+        mask.tofile(f)
+    text = case["info_text"].replace("@DIR@/parts.bin", str(data)).replace("@DIR@/mask.bin", str(mpath))
+    par = annmap.Parameters(text=text.replace("mem_buffer = 1000", "mem_buffer = 333"))
+    reader = annmap.DataReader(par.nativeDatafile, par.isMask, par.maskFileName)
+    reader.setTest(par.testNum)
+    reader.setBuf(par.memParts)
+    reader.open()
+    gen = annmap.MapGenerator(par, reader, precision=precision)
+    gen.start()
+    reader.close()
+    assert gen.isFinished() and gen.getNside() == 32
+    check(gen.getMap(), case["map"], precision)
+
+
+@pytest.mark.parametrize("precision", [PLAIN, COMP])
+def test_synthetic_vs_oracle(rend, precision):
+    P = synth.nfw_halo(20000, seed=5150, n_sub=12)
+    nside = 256
+    par = annmap.Parameters.for_synthetic(P, nside)
+    o = O.make_params(nside=nside, obs_pos=P.obs_pos, centerpos=P.centerpos, align_vec=P.align_vec,
+                      particle_masses=(P.particle_mass,))
+    ref, ost, tot = O.render(o, P.as_dict(), nthreads=8)
+    rend.set_params(par)
+    got = rend.render(P.as_dict(), nside, precision)
+    st = rend.stats()
+    med, mx = check(got, ref, precision, total=tot, dOmega=o.dOmega)
+    assert st["deposits"] == ost["deposits"]
+    assert st["n_single"] == ost["single_small"]
+    print(f"precision={precision} median={med:.3e} max={mx:.3e}")
+
+
+def test_comp_vs_plain_full_nside(rend):
+    """Both forms at Nside 2048 on a 2^16-particle prefix of the 16M-particle
+    workload: compensated against plain FP64 (the FP64 reference here)."""
+    P, nside = synth.workload("nfw16m_sub100_ns2048", scale=1 / 256)
+    par = annmap.Parameters.for_synthetic(P, nside)
+    rend.set_params(par)
+    plain = rend.render(P.as_dict(), nside, PLAIN)
+    tp = rend.stats()
+    comp = rend.render(P.as_dict(), nside, COMP)
+    tc = rend.stats()
+    assert np.array_equal(plain != 0, comp != 0)
+    med, mx = rel_errors(comp, plain)
+    assert med <= 1e-5 and mx <= 1e-4, (med, mx)
+    dom = par.map.dOmega
+    assert math.isclose(plain.sum() * dom, tp["total_flux"], rel_tol=1e-12)
+    assert math.isclose(comp.sum() * dom, tc["total_flux"], rel_tol=1e-9)
+    assert tp["deposits"] == tc["deposits"]
+    print(f"nside 2048: median={med:.3e} max={mx:.3e} deposits={tc['deposits']} "
+          f"plain {tp['kernel_ms']:.1f} ms comp {tc['kernel_ms']:.1f} ms")
+
+
+@pytest.mark.parametrize("precision", [PLAIN, COMP])
+def test_streaming_equals_single_call(rend, precision):
+    P = synth.nfw_halo(6000, seed=77, n_sub=4)
+    nside = 128
+    par = annmap.Parameters.for_synthetic(P, nside)
+    rend.set_params(par)
+    one = rend.render(P.as_dict(), nside, precision)
+    rend.begin(nside, precision)
+    d = P.as_dict()
+    for i0 in range(0, len(P), 1700):
+        rend.add({k: v[i0:i0 + 1700] for k, v in d.items()})
+    rend.add({k: v[:0] for k, v in d.items()})  # an empty chunk
+    two = rend.end()
+    np.testing.assert_allclose(two, one, rtol=1e-12, atol=0)
+    acc = rend.render(P.as_dict(), nside, precision, out=one.copy(), accumulate=True)
+    np.testing.assert_allclose(acc, 2 * one, rtol=1e-12)
+
+
+def test_device_inputs_and_output(rend):
+    torch = pytest.importorskip("torch")
+    P = synth.nfw_halo(5000, seed=99)
+    nside = 128
+    par = annmap.Parameters.for_synthetic(P, nside)
+    rend.set_params(par)
+    host = rend.render(P.as_dict(), nside, COMP)
+    dev = {k: torch.from_numpy(v).cuda() for k, v in P.as_dict().items()}
+    out = torch.zeros(12 * nside * nside, dtype=torch.float64, device="cuda")
+    rend.render(dev, nside, COMP, out=out)
+    torch.cuda.synchronize()
+    np.testing.assert_allclose(out.cpu().numpy(), host, rtol=1e-12)
+
+
+def test_edge_cases(rend):
+    nside = 64
+    P = synth.nfw_halo(300, seed=3)
+    par = annmap.Parameters.for_synthetic(P, nside)
+    rend.set_params(par)
+    d = P.as_dict()
+    # empty input: an all-zero map
+    empty = rend.render({k: v[:0] for k, v in d.items()}, nside, COMP)
+    assert not empty.any() and rend.stats()["n_in"] == 0
+    # all particles masked (rho < 0): nothing kept
+    masked = dict(d, rho=-np.abs(d["rho"]))
+    mp = rend.render(masked, nside, COMP)
+    assert not mp.any() and rend.stats()["n_kept"] == 0
+    # degenerate particles: at the observer, NaN / negative / infinite h
+    o = np.array(P.obs_pos, np.float32)
+    bad = {k: v[:4].copy() for k, v in d.items()}
+    bad["x"][0], bad["y"][0], bad["z"][0] = o
+    bad["h"][1] = np.nan
+    bad["h"][2] = -1.0
+    bad["h"][3] = np.inf
+    mp = rend.render(bad, nside, COMP)
+    st = rend.stats()
+    assert np.all(np.isfinite(mp)) and st["n_invalid"] == 4 and not mp.any()
+    # one all-sky particle (2 ar > pi): every pixel receives flux
+    one = {k: v[:1].copy() for k, v in d.items()}
+    one["x"][0], one["y"][0], one["z"][0] = o + np.float32(0.05)
+    one["h"][0] = 2.0
+    for prec in (PLAIN, COMP):
+        mp = rend.render(one, nside, prec)
+        assert np.all(mp > 0)
+        assert math.isclose(mp.sum() * par.map.dOmega, rend.stats()["total_flux"], rel_tol=1e-9)
+
+
+def test_invalid_arguments(rend):
+    P = synth.nfw_halo(100, seed=4)
+    par = annmap.Parameters.for_synthetic(P, 16)
+    rend.set_params(par)
+    with pytest.raises(annmap.DmannError):
+        rend.render(P.as_dict(), 0, COMP)
+    with pytest.raises(annmap.DmannError):
+        rend.render(P.as_dict(), 16385, COMP)
+    with pytest.raises(annmap.DmannError):
+        rend.render(P.as_dict(), 16, 7)
+    with pytest.raises(annmap.DmannError):
+        rend.set_units(-1.0)
+    with pytest.raises(annmap.DmannError):
+        rend.set_observer((1, 1, 1), (1, 1, 1), (0, 0, 1))
+    # the context stays usable after errors
+    rend.set_params(par)
+    assert rend.render(P.as_dict(), 16, COMP).sum() > 0
