@@ -44,7 +44,10 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default=WORKLOAD)
-    ap.add_argument("--scale", type=float, default=1.0, help="fraction of the workload's particles")
+    ap.add_argument("--scale", type=float, default=1.0, help="generate a halo with this fraction of "
+                    "the particles (particles get fatter: same halo mass)")
+    ap.add_argument("--subset", type=int, default=0, help="render only the first N particles of the "
+                    "full (shuffled) workload: same per-particle disc statistics")
     ap.add_argument("--plain-scale", type=float, default=1.0 / 64)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-extras", action="store_true", help="skip plain form, e2e and CPU legs")
@@ -189,6 +192,8 @@ def run_reference(args, ws, rank):
         return
     from annmap import synth
     P, nside = synth.workload(args.workload, scale=args.scale)
+    if args.subset:
+        P = P.subset(slice(0, args.subset))
     threads = os.cpu_count() or 1
     per_step = max(2.0, min(20.0, 150.0 / max(1, args.steps + args.warmup)))
     vals = []
@@ -219,6 +224,8 @@ def run_gb300(args, ws, rank, local):
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
     P, nside = synth.workload(args.workload, scale=args.scale)
+    if args.subset:
+        P = P.subset(slice(0, args.subset))
     n = len(P)
     npix = 12 * nside * nside
     par = annmap.Parameters.for_synthetic(P, nside)
@@ -256,7 +263,8 @@ def run_gb300(args, ws, rank, local):
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded NFW host + 100 subhalos; reference data unavailable)",
-            "config": {"workload": args.workload, "particles": n, "nside": nside,
+            "config": {"workload": args.workload + (f" (first {n} particles)" if args.subset else ""),
+                       "particles": n, "nside": nside,
                        "form": "compensated FP32 (FP64 geometry, FP32 weights, two-float sums)",
                        "parallelism": f"replicas x{ws}",
                        "l2": "no flush: inputs 403 MB + map/planes 805 MB > 126 MB L2"},

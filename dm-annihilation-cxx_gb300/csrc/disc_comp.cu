@@ -38,10 +38,11 @@ struct CompForm {
     struct alignas(16) Seg {
         int start, nr, lo, off;
         float A, B, d0, step;
+        float A2, pad0, pad1, pad2;
     };
     struct SegReg {
         int start, nr, lo;
-        float A, B, d0, step;
+        float A, B, d0, step, A2;
     };
     struct Ext {
         float K;
@@ -88,7 +89,17 @@ struct CompForm {
         s.B = (float)(a.rt.st[ring] * d.sth0);
         const double step = kTwoPi / (double)s.nr;
         s.step = (float)step;
-        s.d0 = (float)(((double)lo + shift) * step - d.phi0);
+        // azimuth of the run's first pixel relative to the particle, in
+        // [-pi, pi): runs that were shifted by -nr (disc across phi = 2 pi)
+        // would otherwise start 2 pi low
+        double d0 = ((double)lo + shift) * step - d.phi0;
+        if (d0 < -kPi) d0 += kTwoPi;
+        if (d0 >= kPi) d0 -= kTwoPi;
+        s.d0 = (float)d0;
+        // hav of the ring's colatitude distance to the particle's antipode
+        const float dth2 = (float)(a.rt.theta[ring] + d.theta0 - kPi);
+        const float sb = sinf(0.5f * dth2);
+        s.A2 = sb * sb;
     }
 
     __device__ static void load_seg(const Seg &s, SegReg &r) {
@@ -101,14 +112,14 @@ struct CompForm {
         r.B = f4.y;
         r.d0 = f4.z;
         r.step = f4.w;
+        r.A2 = s.A2;
     }
 
-    __device__ static float weight(const Ext &e, const SegReg &sr, int j) {
-        const float dphi = fmaf((float)j, sr.step, sr.d0);
-        const float x = 0.5f * dphi;
+    // sin x for |x| <= pi/2 (Taylor to x^15) or |x| < 0.35 (to x^7)
+    __device__ static float sin_poly(float x, bool small) {
         const float x2 = x * x;
         float p;
-        if (e.small_x) {
+        if (small) {
             p = fmaf(x2, -1.0f / 5040.0f, 1.0f / 120.0f);
             p = fmaf(x2, p, -1.0f / 6.0f);
             p = fmaf(x2, p, 1.0f);
@@ -121,7 +132,16 @@ struct CompForm {
             p = fmaf(x2, p, -1.0f / 6.0f);
             p = fmaf(x2, p, 1.0f);
         }
-        const float sn = x * p;
+        return x * p;
+    }
+
+    // theta^2 / 4 = asin^2(sqrt(hav theta)).  Beyond 90 degrees (hav > 1/2)
+    // asin(sqrt(h)) loses precision as h -> 1, so the distance is taken to the
+    // particle's antipode instead (same haversine form, ring term A2 and the
+    // azimuth offset dphi -+ pi) and theta = pi - theta'.
+    __device__ static float weight(const Ext &e, const SegReg &sr, int j) {
+        const float dphi = fmaf((float)j, sr.step, sr.d0);
+        const float sn = sin_poly(0.5f * dphi, e.small_x);
         const float h = fmaf(sr.B, sn * sn, sr.A);
         float g;
         if (e.small_h) {
@@ -131,8 +151,15 @@ struct CompForm {
             q = fmaf(h, q, 1.0f);
             g = h * q;
         } else {
-            const float hc = fminf(fmaxf(h, 0.0f), 1.0f);
-            const float t = asinf(sqrtf(hc));
+            float t;
+            if (h <= 0.5f) {
+                t = asinf(sqrtf(fmaxf(h, 0.0f)));
+            } else {
+                const float dpf = dphi - copysignf(3.14159265358979f, dphi);
+                const float sf = sin_poly(0.5f * dpf, false);
+                const float hf = fmaf(sr.B, sf * sf, sr.A2);
+                t = 1.57079632679490f - asinf(sqrtf(fminf(fmaxf(hf, 0.0f), 1.0f)));
+            }
             g = t * t;
         }
         return ex2_approx(-e.K * g);

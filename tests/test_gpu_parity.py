@@ -118,9 +118,11 @@ def test_synthetic_vs_oracle(rend, precision):
 
 
 def test_comp_vs_plain_full_nside(rend):
-    """Both forms at Nside 2048 on a 2^16-particle prefix of the 16M-particle
-    workload: compensated against plain FP64 (the FP64 reference here)."""
+    """Both forms at Nside 2048 on the first 4096 particles of a 2^16-particle
+    version of the 16M-particle workload (fatter particles: about 3.6e6 disc
+    pixels each): compensated against plain FP64 (the FP64 reference here)."""
     P, nside = synth.workload("nfw16m_sub100_ns2048", scale=1 / 256)
+    P = P.subset(slice(0, 4096))
     par = annmap.Parameters.for_synthetic(P, nside)
     rend.set_params(par)
     plain = rend.render(P.as_dict(), nside, PLAIN)
@@ -151,9 +153,12 @@ def test_streaming_equals_single_call(rend, precision):
         rend.add({k: v[i0:i0 + 1700] for k, v in d.items()})
     rend.add({k: v[:0] for k, v in d.items()})  # an empty chunk
     two = rend.end()
-    np.testing.assert_allclose(two, one, rtol=1e-12, atol=0)
+    # chunking changes only the order of the additions: FP64 atomics round at
+    # 1e-16, the compensated planes' lo part rounds at ~1e-11 of a pixel
+    tol = 1e-12 if precision == PLAIN else 1e-10
+    np.testing.assert_allclose(two, one, rtol=tol, atol=0)
     acc = rend.render(P.as_dict(), nside, precision, out=one.copy(), accumulate=True)
-    np.testing.assert_allclose(acc, 2 * one, rtol=1e-12)
+    np.testing.assert_allclose(acc, 2 * one, rtol=tol)
 
 
 def test_device_inputs_and_output(rend):
