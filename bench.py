@@ -237,12 +237,14 @@ def run_gb300(args, ws, rank, local):
     stream = torch.cuda.current_stream(dev)
     r.set_stream(stream)
 
-    for _ in range(args.warmup):
-        r.render(dparts, nside, annmap.COMP_F32, out=dmap)
-    torch.cuda.synchronize()
-    disc_ms, step_stats = [], None
+    disc_ms, step_ms, step_stats = [], [], None
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    # the clock sampler starts before the warm-up so its start-up is not timed
     with ClockSampler(local) as clk:
+        for _ in range(args.warmup):
+            r.render(dparts, nside, annmap.COMP_F32, out=dmap)
+        torch.cuda.synchronize()
+        clk.lines.clear()
         barrier(ws)
         torch.cuda.synchronize()
         e0.record(stream)
@@ -250,6 +252,7 @@ def run_gb300(args, ws, rank, local):
             r.render(dparts, nside, annmap.COMP_F32, out=dmap)
             step_stats = r.stats()
             disc_ms.append(step_stats["disc_ms"])
+            step_ms.append(step_stats["kernel_ms"])
         e1.record(stream)
         torch.cuda.synchronize()
         barrier(ws)
@@ -271,7 +274,9 @@ def run_gb300(args, ws, rank, local):
             "clocks": clocks, "gpu_launches": KERNELS_PER_STEP * args.steps,
             "deposits_per_step": step_stats["deposits"],
             "deposits_per_s": step_stats["deposits"] / (ms / 1e3),
-            "stage_ms": {"step": ms, "disc_kernels": statistics.mean(disc_ms)}}
+            "stage_ms": {"step": ms, "disc_kernels": statistics.mean(disc_ms),
+                         "disc_block": step_stats["disc_block_ms"], "disc_warp": step_stats["disc_warp_ms"],
+                         "per_step": [round(x, 2) for x in step_ms]}}
 
     # roofline of the dominant kernels (the disc kernels): one 8-byte
     # read-modify-write reduction per algorithmic deposit

@@ -26,7 +26,7 @@ struct DevBuf {
 };
 
 struct RingTables {
-    double *z = nullptr, *st = nullptr, *theta = nullptr;
+    double *z = nullptr, *st = nullptr, *theta = nullptr, *step = nullptr;
 };
 
 }  // namespace
@@ -36,7 +36,7 @@ struct dmann_ctx {
     int num_sms = 0;
     cudaStream_t own = nullptr;
     cudaStream_t stream = nullptr;
-    cudaEvent_t ev0 = nullptr, ev1 = nullptr, evd0 = nullptr, evd1 = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr, evd0 = nullptr, evdm = nullptr, evd1 = nullptr;
     bool disc_timed = false;
     bool have_frame = false, have_units = false;
     double rot[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
@@ -130,7 +130,7 @@ dmann_status ring_tables(dmann_ctx *ctx, int nside, RingTables &out) {
     }
     const Hpx g = make_hpx(nside);
     const int n = 4 * nside;
-    std::vector<double> z(n, 0.0), st(n, 0.0), th(n, 0.0);
+    std::vector<double> z(n, 0.0), st(n, 0.0), th(n, 0.0), stp(n, 0.0);
     for (int r = 1; r < n; r++) {
         bool have = false;
         double tmp = 0.0;
@@ -148,6 +148,8 @@ dmann_status ring_tables(dmann_ctx *ctx, int nside, RingTables &out) {
         }
         st[r] = have ? std::sqrt(tmp * (2.0 - tmp)) : std::sqrt((1.0 - z[r]) * (1.0 + z[r]));
         th[r] = have ? std::atan2(st[r], z[r]) : std::acos(z[r]);
+        const int nr = r < nside ? 4 * r : (r < 3 * nside ? 4 * nside : 4 * (4 * nside - r));
+        stp[r] = 6.283185307179586476925286766559005768394 / (double)nr;
     }
     RingTables t;
     CK(cudaMalloc(&t.z, sizeof(double) * n));
@@ -156,6 +158,8 @@ dmann_status ring_tables(dmann_ctx *ctx, int nside, RingTables &out) {
     CK(cudaMemcpy(t.z, z.data(), sizeof(double) * n, cudaMemcpyHostToDevice));
     CK(cudaMemcpy(t.st, st.data(), sizeof(double) * n, cudaMemcpyHostToDevice));
     CK(cudaMemcpy(t.theta, th.data(), sizeof(double) * n, cudaMemcpyHostToDevice));
+    CK(cudaMalloc(&t.step, sizeof(double) * n));
+    CK(cudaMemcpy(t.step, stp.data(), sizeof(double) * n, cudaMemcpyHostToDevice));
     ctx->rings[nside] = t;
     out = t;
     return DMANN_OK;
@@ -171,6 +175,9 @@ dmann_status collect_stats(dmann_ctx *ctx) {
     if (ctx->disc_timed) {
         CK(cudaEventElapsedTime(&ms, ctx->evd0, ctx->evd1));
         ctx->stats.disc_ms = ms;
+        CK(cudaEventElapsedTime(&ms, ctx->evd0, ctx->evdm));
+        ctx->stats.disc_block_ms = ms;
+        ctx->stats.disc_warp_ms = ctx->stats.disc_ms - ms;
     }
     ctx->stats.n_kept = ctx->h_ctr[C_KEPT];
     ctx->stats.n_invalid = ctx->h_ctr[C_INVALID];
@@ -208,6 +215,7 @@ dmann_status dmann_create(dmann_ctx **out, int device) {
         cudaStreamCreateWithFlags(&ctx->own, cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreate(&ctx->ev0) != cudaSuccess || cudaEventCreate(&ctx->ev1) != cudaSuccess ||
         cudaEventCreate(&ctx->evd0) != cudaSuccess || cudaEventCreate(&ctx->evd1) != cudaSuccess ||
+        cudaEventCreate(&ctx->evdm) != cudaSuccess ||
         cudaHostAlloc((void **)&ctx->h_ctr, 8 * (C_COUNT + 1), cudaHostAllocDefault) != cudaSuccess) {
         cudaGetLastError();
         delete ctx;
@@ -236,11 +244,13 @@ void dmann_destroy(dmann_ctx *ctx) {
         cudaFree(kv.second.z);
         cudaFree(kv.second.st);
         cudaFree(kv.second.theta);
+        cudaFree(kv.second.step);
     }
     if (ctx->h_ctr) cudaFreeHost(ctx->h_ctr);
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
     if (ctx->evd0) cudaEventDestroy(ctx->evd0);
     if (ctx->evd1) cudaEventDestroy(ctx->evd1);
+    if (ctx->evdm) cudaEventDestroy(ctx->evdm);
     if (ctx->ev1) cudaEventDestroy(ctx->ev1);
     if (ctx->own) cudaStreamDestroy(ctx->own);
     delete ctx;
@@ -439,7 +449,7 @@ dmann_status dmann_map_add(dmann_ctx *ctx, const float *x, const float *y, const
     DiscArgs da;
     da.g = ctx->g;
     da.f = f;
-    da.rt = {ctx->rt.z, ctx->rt.st, ctx->rt.theta};
+    da.rt = {ctx->rt.z, ctx->rt.st, ctx->rt.theta, ctx->rt.step};
     da.theta = pa.out.theta;
     da.phi = pa.out.phi;
     da.ar = pa.out.ar;
@@ -449,8 +459,8 @@ dmann_status dmann_map_add(dmann_ctx *ctx, const float *x, const float *y, const
     da.ctr = pa.ctr;
     da.acc = acc;
     CK(cudaEventRecord(ctx->evd0, s));
-    if (ctx->precision == DMANN_PLAIN_F64) CK(launch_disc_plain(da, ctx->num_sms, ctx->tune.blocks_per_sm, s));
-    else CK(launch_disc_comp(da, ctx->num_sms, ctx->tune.blocks_per_sm, s));
+    if (ctx->precision == DMANN_PLAIN_F64) CK(launch_disc_plain(da, ctx->num_sms, ctx->tune.blocks_per_sm, s, ctx->evdm));
+    else CK(launch_disc_comp(da, ctx->num_sms, ctx->tune.blocks_per_sm, s, ctx->evdm));
     CK(cudaEventRecord(ctx->evd1, s));
     ctx->disc_timed = true;
     return DMANN_OK;

@@ -44,6 +44,7 @@ struct RingTab {
     const double *z;
     const double *st;
     const double *theta;
+    const double *step;   // 2 pi / (pixels in the ring)
 };
 
 __host__ __device__ inline int64_t ring_start(const Hpx &g, int ring) {
@@ -178,8 +179,29 @@ __device__ inline void disc_setup(const Hpx &g, double theta, double phi, double
 // negative; indices wrap modulo nr).  Full rings (pole inside the disc, or
 // the all-sky case) start at the pixel nearest phi0 - pi so that, walking
 // forward, phi - phi0 stays in [-pi, pi).
+// Fast variant of the chord test: the chord half-width dphi is computed in
+// FP32 (atan2f on the FP64 x and y^2 the exact test forms).  Against the
+// FP64 dphi it errs by at most 3.6e-7 dphi (atan2f, 3 ulp) + 3.8e-8 rad (x
+// and sqrt(y^2) rounded to FP32) < 2e-6 rad, which moves the run's end
+// points nr/2pi * (phi0 -+ dphi) - shift by less than tau = nr/2pi * 2e-6.
+// Only when an end point lies within tau of an integer can its floor differ,
+// and then the exact FP64 formula decides.  The pixel runs are therefore
+// identical to the exact test's.
+template <bool kFast>
+__device__ inline void ring_segment_t(const Hpx &g, const DiscHdr &d, int ring, int &lo, int &cnt);
+
 __device__ inline void ring_segment(const Hpx &g, const DiscHdr &d, int ring, int &lo,
                                     int &cnt) {
+    ring_segment_t<false>(g, d, ring, lo, cnt);
+}
+
+__device__ inline bool near_integer(double a, double tau) {
+    const double fr = a - floor(a);
+    return fr < tau || fr > 1.0 - tau;
+}
+
+template <bool kFast>
+__device__ inline void ring_segment_t(const Hpx &g, const DiscHdr &d, int ring, int &lo, int &cnt) {
     const int nr = ring_npix(g, ring);
     const double shift = ring_shifted(g, ring) ? 0.5 : 0.0;
     if (d.allsky || ring < d.irmin || ring > d.irmax) {
@@ -192,13 +214,26 @@ __device__ inline void ring_segment(const Hpx &g, const DiscHdr &d, int ring, in
     double z = ring2z(g, ring);
     double x = __dmul_rn(__dsub_rn(d.cosR, __dmul_rn(z, d.z0)), d.xa);
     double ysq = __dsub_rn(__dsub_rn(1.0, __dmul_rn(z, z)), __dmul_rn(x, x));
-    double dphi = (ysq <= 0) ? 0.0 : atan2(__dsqrt_rn(ysq), x);
     lo = 0;
     cnt = 0;
-    if (dphi > 0) {
-        double fnr = __dmul_rn((double)nr, kInvTwoPi);
-        int ip_lo = (int)floor(__dsub_rn(__dmul_rn(fnr, __dsub_rn(d.phi0, dphi)), shift)) + 1;
-        int ip_hi = (int)floor(__dsub_rn(__dmul_rn(fnr, __dadd_rn(d.phi0, dphi)), shift));
+    if (ysq > 0) {
+        const double fnr = __dmul_rn((double)nr, kInvTwoPi);
+        double a_lo, a_hi;
+        bool exact = !kFast;
+        if (kFast) {
+            const double dphif = (double)atan2f(sqrtf((float)ysq), (float)x);
+            a_lo = __dsub_rn(__dmul_rn(fnr, __dsub_rn(d.phi0, dphif)), shift);
+            a_hi = __dsub_rn(__dmul_rn(fnr, __dadd_rn(d.phi0, dphif)), shift);
+            const double tau = fnr * 2.0e-6 + 1e-9;
+            exact = near_integer(a_lo, tau) || near_integer(a_hi, tau);
+        }
+        if (exact) {
+            const double dphi = atan2(__dsqrt_rn(ysq), x);
+            a_lo = __dsub_rn(__dmul_rn(fnr, __dsub_rn(d.phi0, dphi)), shift);
+            a_hi = __dsub_rn(__dmul_rn(fnr, __dadd_rn(d.phi0, dphi)), shift);
+        }
+        int ip_lo = (int)floor(a_lo) + 1;
+        int ip_hi = (int)floor(a_hi);
         if (ip_lo <= ip_hi) {
             if (ip_hi >= nr) { ip_lo -= nr; ip_hi -= nr; }
             lo = ip_lo;

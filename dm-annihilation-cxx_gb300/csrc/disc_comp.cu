@@ -35,6 +35,7 @@ __device__ __forceinline__ float ex2_approx(float x) {
 }
 
 struct CompForm {
+    static constexpr bool kFastChord = true;
     struct alignas(16) Seg {
         int start, nr, lo, off;
         float A, B, d0, step;
@@ -87,7 +88,7 @@ struct CompForm {
         const float sa = sinf(0.5f * dth);
         s.A = sa * sa;
         s.B = (float)(a.rt.st[ring] * d.sth0);
-        const double step = kTwoPi / (double)s.nr;
+        const double step = a.rt.step[ring];
         s.step = (float)step;
         // azimuth of the run's first pixel relative to the particle, in
         // [-pi, pi): runs that were shifted by -nr (disc across phi = 2 pi)
@@ -201,12 +202,13 @@ struct CompForm {
     }
 };
 
-constexpr int kBT = 256, kRCH = 256;
+constexpr int kBT = 256, kRCH = 512;
 constexpr int kWPB = 8, kRCHW = 64;
 
 }  // namespace
 
-cudaError_t launch_disc_comp(const DiscArgs &a, int num_sms, int blocks_per_sm, cudaStream_t s) {
+cudaError_t launch_disc_comp(const DiscArgs &a, int num_sms, int blocks_per_sm, cudaStream_t s,
+                             cudaEvent_t mid) {
     int occ = 0;
     cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
         &occ, k_disc_block<CompForm, kBT, kRCH>, kBT, 0);
@@ -216,6 +218,7 @@ cudaError_t launch_disc_comp(const DiscArgs &a, int num_sms, int blocks_per_sm, 
     k_disc_block<CompForm, kBT, kRCH><<<num_sms * bps, kBT, 0, s>>>(a);
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
+    if (mid && (e = cudaEventRecord(mid, s)) != cudaSuccess) return e;
     int occw = 0;
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occw, k_disc_warp<CompForm, kWPB, kRCHW>,
                                                       kWPB * 32, 0);

@@ -92,7 +92,7 @@ __device__ inline void build_chunk(const DiscArgs &a, GroupSmem<Form, RCH> &sm, 
     for (int i = Grp::rank(); i < n; i += G) {
         const int ring = r0 + i;
         int lo, cnt;
-        ring_segment(a.g, sm.hdr, ring, lo, cnt);
+        ring_segment_t<Form::kFastChord>(a.g, sm.hdr, ring, lo, cnt);
         Form::fill_seg(a, sm.hdr, sm.ext, ring, lo, cnt, sm.seg[i]);
         sm.seg[i].off = cnt;
     }

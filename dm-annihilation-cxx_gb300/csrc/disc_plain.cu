@@ -14,6 +14,7 @@ namespace dmann {
 namespace {
 
 struct PlainForm {
+    static constexpr bool kFastChord = false;  // the exact FP64 chord test
     struct alignas(16) Seg {
         int start, nr, lo, off;
         double z, st, pf;
@@ -117,7 +118,8 @@ constexpr int kWPB = 8, kRCHW = 64;
 
 }  // namespace
 
-cudaError_t launch_disc_plain(const DiscArgs &a, int num_sms, int blocks_per_sm, cudaStream_t s) {
+cudaError_t launch_disc_plain(const DiscArgs &a, int num_sms, int blocks_per_sm, cudaStream_t s,
+                              cudaEvent_t mid) {
     int occ = 0;
     cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
         &occ, k_disc_block<PlainForm, kBT, kRCH>, kBT, 0);
@@ -127,6 +129,7 @@ cudaError_t launch_disc_plain(const DiscArgs &a, int num_sms, int blocks_per_sm,
     k_disc_block<PlainForm, kBT, kRCH><<<num_sms * bps, kBT, 0, s>>>(a);
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
+    if (mid && (e = cudaEventRecord(mid, s)) != cudaSuccess) return e;
     int occw = 0;
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occw, k_disc_warp<PlainForm, kWPB, kRCHW>,
                                                       kWPB * 32, 0);

@@ -74,7 +74,11 @@ cudaError_t launch_scatter(const PrepArgs &a, int *queue, cudaStream_t s);
 cudaError_t launch_finalize(const Accum &acc, int precision, int npix, double dOmega,
                             double scale, double *out, int accumulate, cudaStream_t s);
 // disc_plain.cu / disc_comp.cu
-cudaError_t launch_disc_plain(const DiscArgs &a, int num_sms, int blocks_per_sm, cudaStream_t s);
-cudaError_t launch_disc_comp(const DiscArgs &a, int num_sms, int blocks_per_sm, cudaStream_t s);
+// Launch the block-per-particle kernel, record `mid` (if not null), then the
+// warp-per-particle kernel.
+cudaError_t launch_disc_plain(const DiscArgs &a, int num_sms, int blocks_per_sm, cudaStream_t s,
+                              cudaEvent_t mid);
+cudaError_t launch_disc_comp(const DiscArgs &a, int num_sms, int blocks_per_sm, cudaStream_t s,
+                             cudaEvent_t mid);
 
 }  // namespace dmann

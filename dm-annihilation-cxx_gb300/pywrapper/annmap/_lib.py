@@ -29,6 +29,7 @@ class Stats(C.Structure):
                 ("n_single", C.c_int64),
                 ("n_disc", C.c_int64), ("n_disc_block", C.c_int64), ("deposits", C.c_int64),
                 ("kernel_ms", C.c_double), ("disc_ms", C.c_double),
+                ("disc_block_ms", C.c_double), ("disc_warp_ms", C.c_double),
                 ("total_flux", C.c_double)]
 
 

@@ -87,6 +87,8 @@ typedef struct {
     int64_t deposits;      /* algorithmic deposits: sum of disc sizes + singles */
     double kernel_ms;      /* device time from map_begin to map_end (events) */
     double disc_ms;        /* device time of the disc kernels of the last chunk */
+    double disc_block_ms;  /* of which the block-per-particle kernel */
+    double disc_warp_ms;   /* of which the warp-per-particle kernel */
     double total_flux;     /* sum of kept flux (before the dOmega division) */
 } dmann_stats;
 

@@ -172,7 +172,8 @@ def test_device_inputs_and_output(rend):
     out = torch.zeros(12 * nside * nside, dtype=torch.float64, device="cuda")
     rend.render(dev, nside, COMP, out=out)
     torch.cuda.synchronize()
-    np.testing.assert_allclose(out.cpu().numpy(), host, rtol=1e-12)
+    # same arithmetic; the atomics' order differs run to run (lo plane ~1e-11)
+    np.testing.assert_allclose(out.cpu().numpy(), host, rtol=1e-10)
 
 
 def test_edge_cases(rend):
@@ -190,6 +191,8 @@ def test_edge_cases(rend):
     assert not mp.any() and rend.stats()["n_kept"] == 0
     # degenerate particles: at the observer, NaN / negative / infinite h
     o = np.array(P.obs_pos, np.float32)
+    # an observer exactly representable in float32, so a particle can sit on it
+    rend.set_frame(par.rotmatrix, o.astype(np.float64))
     bad = {k: v[:4].copy() for k, v in d.items()}
     bad["x"][0], bad["y"][0], bad["z"][0] = o
     bad["h"][1] = np.nan
@@ -198,6 +201,7 @@ def test_edge_cases(rend):
     mp = rend.render(bad, nside, COMP)
     st = rend.stats()
     assert np.all(np.isfinite(mp)) and st["n_invalid"] == 4 and not mp.any()
+    rend.set_params(par)
     # one all-sky particle (2 ar > pi): every pixel receives flux
     one = {k: v[:1].copy() for k, v in d.items()}
     one["x"][0], one["y"][0], one["z"][0] = o + np.float32(0.05)
