@@ -12,8 +12,9 @@ import threading
 PKG_DIR = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
 LIB_PATH = os.path.join(PKG_DIR, "libdmann.so")
 
-OK, ERR_INVALID, ERR_CUDA, ERR_NOMEM, ERR_STATE, ERR_TIMEOUT, ERR_NODEVICE = range(7)
-STATUS_NAMES = {0: "OK", 1: "INVALID", 2: "CUDA", 3: "NOMEM", 4: "STATE", 5: "TIMEOUT", 6: "NODEVICE"}
+OK, ERR_INVALID, ERR_CUDA, ERR_NOMEM, ERR_STATE, ERR_TIMEOUT, ERR_NODEVICE, ERR_TOO_LARGE = range(8)
+STATUS_NAMES = {0: "OK", 1: "INVALID", 2: "CUDA", 3: "NOMEM", 4: "STATE", 5: "TIMEOUT", 6: "NODEVICE",
+                7: "TOO_LARGE"}
 PLAIN_F64, COMP_F32 = 0, 1
 FLUX_ANN_NOSOM = 0
 
@@ -66,6 +67,8 @@ SIGNATURES = {
     "dmann_observer_rotation": (C.c_int, [_D3, _D3, _D3, _D3, _D3]),
     "dmann_code_units": (C.c_int, [C.c_double, C.c_double, C.c_double, _D3]),
     "dmann_hires_threshold": (C.c_double, [_D3, C.c_int]),
+    "dmann_render_noalloc": (C.c_int, [_P, _P, _P, _P, _P, _P, C.c_int64, C.c_int, _D3, _D3,
+                                       C.c_double, C.c_double, _P, C.c_int, _P]),
 }
 
 

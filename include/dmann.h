@@ -55,7 +55,8 @@ typedef enum {
     DMANN_ERR_NOMEM = 3,     /* device or host allocation failed */
     DMANN_ERR_STATE = 4,     /* call order (e.g. render before an observer) */
     DMANN_ERR_TIMEOUT = 5,   /* a bounded device wait gave up */
-    DMANN_ERR_NODEVICE = 6   /* no CUDA device / wrong architecture */
+    DMANN_ERR_NODEVICE = 6,  /* no CUDA device / wrong architecture */
+    DMANN_ERR_TOO_LARGE = 7  /* dmann_render_noalloc: problem exceeds its fixed scratch */
 } dmann_status;
 
 /* Precision forms of the projection. */
@@ -159,6 +160,36 @@ dmann_status dmann_map_end(dmann_ctx *ctx, double *map_out, int accumulate);
 
 /* Statistics of the last completed map (synchronises the stream). */
 dmann_status dmann_get_stats(const dmann_ctx *ctx, dmann_stats *out);
+
+/* ---- rendering without any allocation ---- */
+/* No counterpart in the reference.  For callers that must not allocate GPU
+ * memory -- a plug-in inside a host application whose own allocator has
+ * reserved the device's memory, or a latency-critical loop where cudaMalloc's
+ * implicit synchronisation is not acceptable -- this renders one map with the
+ * compensated-FP32 form using only a fixed scratch array compiled into the
+ * library (DMANN_NOALLOC_SCRATCH_BYTES, held on every GPU that loads the
+ * library until the process exits).  It calls no cudaMalloc, cudaFree or other
+ * allocating routine and needs no context.
+ *
+ * Inputs (float32 SoA, as dmann_render) and map_out (12*nside^2 doubles) must
+ * be device pointers; rot / opos / unit_factor / hires_threshold are what
+ * dmann_set_frame and dmann_set_units take.  Work is queued on `stream`
+ * (a cudaStream_t, NULL = the default stream) of the current device and the
+ * call returns without waiting.  The scratch needed is about
+ *     8 * 12*nside^2 + 44 * n + 128 * nside + 513 KiB   bytes;
+ * a larger problem is rejected with DMANN_ERR_TOO_LARGE (render it in chunks
+ * of particles with accumulate = 1).  The first call on a device looks up the
+ * array's device address (cudaGetSymbolAddress); make that first call before
+ * any stream capture.  All calls on a device share the one array: calls that
+ * overlap on the GPU (different streams or threads) race and corrupt each
+ * other's maps, so serialise them, e.g. on one stream. */
+#define DMANN_NOALLOC_SCRATCH_BYTES (64u * 1024u * 1024u)
+dmann_status dmann_render_noalloc(const float *x, const float *y, const float *z,
+                                  const float *m, const float *rho, const float *h,
+                                  int64_t n, int nside, const double rot[9],
+                                  const double opos[3], double unit_factor,
+                                  double hires_threshold, double *map_out,
+                                  int accumulate, void *stream);
 
 /* ---- host-only helpers (no context, no GPU) ---- */
 /* Parameters::setupParams + setupRotation (src/parameters.cpp:111-152,

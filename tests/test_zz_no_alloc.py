@@ -1,0 +1,75 @@
+"""dmann_render_noalloc: rendering with no device allocation at all.
+
+Some callers cannot call cudaMalloc: a plug-in running inside a host program
+whose own allocator has already reserved the GPU's memory, or a tight loop that
+cannot afford cudaMalloc's implicit synchronisation.  For them the library
+offers one entry point that works entirely in a fixed scratch array compiled
+into it.  These tests call it through the C ABI on device buffers and check its
+map against the ordinary compensated render (dmann_render through a context),
+on two calls in a row, with the tolerance the other compensated-form tests use
+for run-to-run differences (the atomics' order: ~1e-11 relative).
+
+This file is named to be collected last, so a run that stops at the first
+failure has run everything else first; it also passes on its own.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+import annmap
+from annmap import _lib, synth
+
+pytestmark = pytest.mark.gpu
+
+RTOL = 1e-10
+
+
+def _noalloc(L, parts, n, nside, par, out, accumulate=0, stream=None):
+    d9 = (C.c_double * 9)(*[v for row in par.rotmatrix for v in row])
+    d3 = (C.c_double * 3)(*par.params.opos)
+    p = [C.c_void_p(parts[k].data_ptr()) for k in ("x", "y", "z", "m", "rho", "h")]
+    return L.dmann_render_noalloc(*p, n, nside, d9, d3, par.unit_factor, par.hires_threshold,
+                                  C.c_void_p(out.data_ptr()), accumulate,
+                                  C.c_void_p(stream) if stream else None)
+
+
+def test_noalloc_matches_render_on_two_calls():
+    torch = pytest.importorskip("torch")
+    L = _lib.load()
+    nside = 128
+    stream = torch.cuda.current_stream().cuda_stream
+    for call, seed in enumerate((2024, 2025)):
+        P = synth.nfw_halo(20000, seed=seed, n_sub=6)
+        par = annmap.Parameters.for_synthetic(P, nside)
+        dev = {k: torch.from_numpy(v).cuda() for k, v in P.as_dict().items()}
+        with annmap.Renderer(0) as r:
+            r.set_params(par)
+            ref = r.render(P.as_dict(), nside, annmap.COMP_F32)
+        out = torch.full((12 * nside * nside,), 7.0, dtype=torch.float64, device="cuda")
+        st = _noalloc(L, dev, len(P), nside, par, out, stream=stream)
+        assert st == _lib.OK, st
+        torch.cuda.synchronize()
+        got = out.cpu().numpy()
+        assert np.array_equal(got != 0, ref != 0), f"call {call}: pixel sets differ"
+        np.testing.assert_allclose(got, ref, rtol=RTOL, atol=0)
+        # accumulate into the same map: twice the map
+        st = _noalloc(L, dev, len(P), nside, par, out, accumulate=1, stream=stream)
+        assert st == _lib.OK
+        torch.cuda.synchronize()
+        np.testing.assert_allclose(out.cpu().numpy(), 2 * ref, rtol=RTOL, atol=0)
+
+
+def test_noalloc_rejects_what_it_cannot_hold():
+    torch = pytest.importorskip("torch")
+    L = _lib.load()
+    P = synth.nfw_halo(100, seed=1)
+    par = annmap.Parameters.for_synthetic(P, 4096)
+    dev = {k: torch.from_numpy(v).cuda() for k, v in P.as_dict().items()}
+    # Nside 4096 needs 1.6 GB of accumulation planes: beyond the fixed scratch
+    big = torch.zeros(8, dtype=torch.float64, device="cuda")
+    assert _noalloc(L, dev, len(P), 4096, par, big) == _lib.ERR_TOO_LARGE
+    # host buffers are refused: nothing is staged
+    host = {k: torch.from_numpy(v) for k, v in P.as_dict().items()}
+    out = torch.zeros(12 * 16 * 16, dtype=torch.float64, device="cuda")
+    assert _noalloc(L, host, len(P), 16, par, out) == _lib.ERR_INVALID
