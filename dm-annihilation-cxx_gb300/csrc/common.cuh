@@ -254,15 +254,18 @@ __device__ inline double disc_npix_estimate(const Hpx &g, double ar) {
 }
 
 // ---------------------------------------------------------------- atomics
+// The accumulation planes are only read after the kernel, so these carry no
+// "memory" clobber: a clobber would make the compiler reload every loop-
+// invariant value held in shared memory after each deposit.
 __device__ inline void red_add_f64(double *addr, double v) {
-    asm volatile("red.global.add.f64 [%0], %1;" ::"l"(addr), "d"(v) : "memory");
+    asm volatile("red.global.add.f64 [%0], %1;" ::"l"(addr), "d"(v));
 }
 __device__ inline void red_add_f32(float *addr, float v) {
-    asm volatile("red.global.add.f32 [%0], %1;" ::"l"(addr), "f"(v) : "memory");
+    asm volatile("red.global.add.f32 [%0], %1;" ::"l"(addr), "f"(v));
 }
 __device__ inline float atom_add_f32(float *addr, float v) {
     float old;
-    asm volatile("atom.global.add.f32 %0, [%1], %2;" : "=f"(old) : "l"(addr), "f"(v) : "memory");
+    asm volatile("atom.global.add.f32 %0, [%1], %2;" : "=f"(old) : "l"(addr), "f"(v));
     return old;
 }
 

@@ -36,6 +36,7 @@ __device__ __forceinline__ float ex2_approx(float x) {
 
 struct CompForm {
     static constexpr bool kFastChord = true;
+    static constexpr int kMinBlocks = 8;  // 8 x 256 threads per SM: full occupancy
     struct alignas(16) Seg {
         int start, nr, lo, off;
         float A, B, d0, step;

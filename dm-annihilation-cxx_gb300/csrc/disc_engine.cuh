@@ -158,6 +158,7 @@ __device__ inline void render_particle(const DiscArgs &a, GroupSmem<Form, RCH> &
         Form::particle_setup(a, sm.hdr, a.phi[pidx], sm.ext);
     }
     Grp::sync();
+    const typename Form::Ext ext = sm.ext;  // per-particle constants, in registers
     const int r_first = sm.hdr.r_first, r_last = sm.hdr.r_last;
     const int nring = r_last - r_first + 1;
     const int nchunk = nring > 0 ? (nring + RCH - 1) / RCH : 0;
@@ -172,7 +173,7 @@ __device__ inline void render_particle(const DiscArgs &a, GroupSmem<Form, RCH> &
         const int ct = (int)sm.chunk_total;
         total += ct;
         pixel_walk<Form, G, RCH>(sm, n, ct, [&](const typename Form::SegReg &sr, int j, int pix) {
-            Form::norm_add(sm.ext, sr, j, pix, nacc);
+            Form::norm_add(ext, sr, j, pix, nacc);
         });
         Grp::sync();
     }
@@ -196,7 +197,7 @@ __device__ inline void render_particle(const DiscArgs &a, GroupSmem<Form, RCH> &
     }
     if (r == 0) atomicAdd((unsigned long long *)(a.ctr + C_DEPOSITS), (unsigned long long)total);
     typename Form::Dep dep;
-    Form::deposit_setup(a, sm.hdr, sm.ext, S, dep);
+    Form::deposit_setup(a, sm.hdr, ext, S, dep);
 
     // pass 2: deposits (the staged chunk is reused when there is only one)
     for (int c = 0; c < nchunk; c++) {
@@ -205,16 +206,19 @@ __device__ inline void render_particle(const DiscArgs &a, GroupSmem<Form, RCH> &
         if (nchunk > 1) build_chunk<Form, G, RCH>(a, sm, r0, n);
         const int ct = (int)sm.chunk_total;
         pixel_walk<Form, G, RCH>(sm, n, ct, [&](const typename Form::SegReg &sr, int j, int pix) {
-            Form::deposit(a, sm.ext, dep, sr, j, pix);
+            Form::deposit(a, ext, dep, sr, j, pix);
         });
         Grp::sync();
     }
 }
 
 // One thread block per particle, persistent over the block-class queue
-// (largest discs first, claimed dynamically).
+// (largest discs first, claimed dynamically).  Form::kMinBlocks resident
+// blocks per SM are asked of the compiler: the compensated kernel is latency
+// bound (returned atomics), and full occupancy measured fastest even with
+// some register spilling.
 template <class Form, int BT, int RCH>
-__global__ void __launch_bounds__(BT) k_disc_block(DiscArgs a) {
+__global__ void __launch_bounds__(BT, Form::kMinBlocks) k_disc_block(DiscArgs a) {
     __shared__ GroupSmem<Form, RCH> sm;
     __shared__ int s_q;
     const long long nblk = a.ctr[C_ADD_BLOCK];

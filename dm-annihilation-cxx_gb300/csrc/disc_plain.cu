@@ -15,6 +15,7 @@ namespace {
 
 struct PlainForm {
     static constexpr bool kFastChord = false;  // the exact FP64 chord test
+    static constexpr int kMinBlocks = 1;
     struct alignas(16) Seg {
         int start, nr, lo, off;
         double z, st, pf;
