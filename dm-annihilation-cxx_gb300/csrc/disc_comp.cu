@@ -1,20 +1,30 @@
 // disc_comp.cu -- the compensated-FP32 form of the disc kernels.
 //
 // Per particle (FP64, once): direction, angular radius, disc rings and each
-// ring's in-disc pixel run (the query_disc chord test, exactly the CPU
-// path's arithmetic).  Per pixel (FP32): the angular distance to the particle
-// from the haversine relation
+// ring's in-disc pixel run (the query_disc chord test; FP32 with an exact FP64
+// fallback near ties, so the pixel sets equal the CPU path's).  Per pixel
+// (FP32): the angular distance to the particle from the haversine relation
 //     hav(theta) = hav(theta_ring - theta0) + sin(theta_ring) sin(theta0) hav(dphi)
 // (well conditioned at the small angles where acos(dot) is not), then
 // theta^2 = 4 asin^2(sqrt(hav)) and w = 2^(-K theta^2) with
 // K = log2(e) * 0.5 / (0.333 ar^2): the reference's exp(-0.5 (theta/ar)^2 /
-// 0.333) (src/genmap.cpp:137-143).  The per-ring terms hav(theta_r - theta0)
-// and sin(theta_r) sin(theta0), and the first pixel's azimuth offset, are
-// formed in FP64 and rounded once, so the FP32 error does not grow with the
-// absolute angles.  The normalisation is a Kahan-compensated FP32 sum per
-// thread, reduced in FP64; deposits go to two FP32 planes (hi, lo) with an
-// exact TwoSum on the value each atomic returns, plus the product's own
-// rounding error.
+// 0.333) (src/genmap.cpp:137-143).  The per-ring terms hav(theta_r - theta0),
+// sin(theta_r) sin(theta0) and the run's first azimuth offset are formed in
+// FP64 and rounded once, so the FP32 error does not grow with the absolute
+// angles.  Beyond 90 degrees (hav > 1/2) the distance is taken to the
+// particle's antipode, where asin(sqrt(h)) would lose precision.
+//
+// Normalisation: a Kahan-compensated FP32 sum per thread, reduced in FP64.
+// Deposits: two FP32 planes (hi, lo); the hi atomic returns the old value, so
+// the exact TwoSum error of each addition -- plus the product's own rounding
+// error and the low part of flux/norm -- goes to the lo plane.
+//
+// Work layout ("run engine"): the disc's rings are staged in shared memory
+// as runs -- one ring's in-disc pixels, split where the ring wraps so that a
+// run is contiguous in the map -- and each warp takes whole runs.  A lane
+// evaluates two pixels of a run at once (j and j + 32) with the packed FP32x2
+// instructions of sm_100+ (__ffma2_rn & co.), halving the issue slots of the
+// polynomial, Kahan and TwoSum arithmetic.
 //
 // Polynomials (written from their Taylor series):
 //   sin x = x - x^3/3! + x^5/5! - ... ; to x^7 for |x| < 0.35 (error
@@ -22,7 +32,7 @@
 //   asin^2(sqrt h) = sum_n (4h)^n / (2 n^2 C(2n,n)) = h + h^2/3 + 8h^3/45 +
 //   4h^4/35 + 128h^5/1575 + ... ; five terms for h < 0.02 (error < 3e-10
 //   relative); otherwise asinf(sqrtf(h)) from the CUDA math library.
-#include "disc_engine.cuh"
+#include "kernels.cuh"
 
 namespace dmann {
 
@@ -34,198 +44,336 @@ __device__ __forceinline__ float ex2_approx(float x) {
     return y;
 }
 
-struct CompForm {
-    static constexpr bool kFastChord = true;
-    static constexpr int kMinBlocks = 8;  // 8 x 256 threads per SM: full occupancy
-    struct alignas(16) Seg {
-        int start, nr, lo, off;
-        float A, B, d0, step;
-        float A2, pad0, pad1, pad2;
-    };
-    struct SegReg {
-        int start, nr, lo;
-        float A, B, d0, step, A2;
-    };
-    struct Ext {
-        float K;
-        int small_h, small_x;
-    };
-    struct NormAcc {
-        float s = 0.0f, c = 0.0f;
-    };
-    struct Dep {
-        float F, Flo;   // flux/norm as a two-float
-    };
+// packed FP32x2 arithmetic (round to nearest per element)
+__device__ __forceinline__ float2 f2(float v) { return make_float2(v, v); }
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) {
+    return __fadd2_rn(a, make_float2(-b.x, -b.y));
+}
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
 
-    __device__ static void particle_setup(const DiscArgs &a, const DiscHdr &d, double phi_raw,
-                                          Ext &e) {
-        (void)a;
-        (void)phi_raw;
-        e.K = (float)(4.0 * 1.4426950408889634 * 0.5 / (0.333 * d.ar * d.ar));
-        double hmax = 1.0;
-        if (!d.allsky) {
-            double s = sin(0.5 * d.R);
-            hmax = s * s;
-        }
-        e.small_h = hmax < 0.02;
-        bool caps = d.allsky || d.r_first < d.irmin || d.r_last > d.irmax;
-        int small_x = 0;
-        if (!caps) {
-            double sr = sin(d.R);
-            if (sr < 0.999 * d.sth0) small_x = (0.5 * asin(sr / d.sth0)) < 0.33;
-        }
-        e.small_x = small_x;
-    }
+constexpr float kHalfPiF = 1.57079632679490f;
 
-    __device__ static void fill_seg(const DiscArgs &a, const DiscHdr &d, const Ext &e, int ring,
-                                    int lo, int cnt, Seg &s) {
-        (void)e;
-        (void)cnt;
-        s.start = (int)ring_start(a.g, ring);
-        s.nr = ring_npix(a.g, ring);
-        s.lo = lo;
-        const double shift = ring_shifted(a.g, ring) ? 0.5 : 0.0;
-        const float dth = (float)(a.rt.theta[ring] - d.theta0);
-        const float sa = sinf(0.5f * dth);
-        s.A = sa * sa;
-        s.B = (float)(a.rt.st[ring] * d.sth0);
-        const double step = a.rt.step[ring];
-        s.step = (float)step;
-        // azimuth of the run's first pixel relative to the particle, in
-        // [-pi, pi): runs that were shifted by -nr (disc across phi = 2 pi)
-        // would otherwise start 2 pi low
-        double d0 = ((double)lo + shift) * step - d.phi0;
-        if (d0 < -kPi) d0 += kTwoPi;
-        if (d0 >= kPi) d0 -= kTwoPi;
-        s.d0 = (float)d0;
-        // hav of the ring's colatitude distance to the particle's antipode
-        const float dth2 = (float)(a.rt.theta[ring] + d.theta0 - kPi);
-        const float sb = sinf(0.5f * dth2);
-        s.A2 = sb * sb;
-    }
-
-    __device__ static void load_seg(const Seg &s, SegReg &r) {
-        const int4 i4 = *reinterpret_cast<const int4 *>(&s.start);
-        const float4 f4 = *reinterpret_cast<const float4 *>(&s.A);
-        r.start = i4.x;
-        r.nr = i4.y;
-        r.lo = i4.z;
-        r.A = f4.x;
-        r.B = f4.y;
-        r.d0 = f4.z;
-        r.step = f4.w;
-        r.A2 = s.A2;
-    }
-
-    // sin x for |x| <= pi/2 (Taylor to x^15) or |x| < 0.35 (to x^7)
-    __device__ static float sin_poly(float x, bool small) {
-        const float x2 = x * x;
-        float p;
-        if (small) {
-            p = fmaf(x2, -1.0f / 5040.0f, 1.0f / 120.0f);
-            p = fmaf(x2, p, -1.0f / 6.0f);
-            p = fmaf(x2, p, 1.0f);
-        } else {
-            p = fmaf(x2, -1.0f / 1307674368000.0f, 1.0f / 6227020800.0f);
-            p = fmaf(x2, p, -1.0f / 39916800.0f);
-            p = fmaf(x2, p, 1.0f / 362880.0f);
-            p = fmaf(x2, p, -1.0f / 5040.0f);
-            p = fmaf(x2, p, 1.0f / 120.0f);
-            p = fmaf(x2, p, -1.0f / 6.0f);
-            p = fmaf(x2, p, 1.0f);
-        }
-        return x * p;
-    }
-
-    // theta^2 / 4 = asin^2(sqrt(hav theta)).  Beyond 90 degrees (hav > 1/2)
-    // asin(sqrt(h)) loses precision as h -> 1, so the distance is taken to the
-    // particle's antipode instead (same haversine form, ring term A2 and the
-    // azimuth offset dphi -+ pi) and theta = pi - theta'.
-    __device__ static float weight(const Ext &e, const SegReg &sr, int j) {
-        const float dphi = fmaf((float)j, sr.step, sr.d0);
-        const float sn = sin_poly(0.5f * dphi, e.small_x);
-        const float h = fmaf(sr.B, sn * sn, sr.A);
-        float g;
-        if (e.small_h) {
-            float q = fmaf(h, 128.0f / 1575.0f, 4.0f / 35.0f);
-            q = fmaf(h, q, 8.0f / 45.0f);
-            q = fmaf(h, q, 1.0f / 3.0f);
-            q = fmaf(h, q, 1.0f);
-            g = h * q;
-        } else {
-            float t;
-            if (h <= 0.5f) {
-                t = asinf(sqrtf(fmaxf(h, 0.0f)));
-            } else {
-                const float dpf = dphi - copysignf(3.14159265358979f, dphi);
-                const float sf = sin_poly(0.5f * dpf, false);
-                const float hf = fmaf(sr.B, sf * sf, sr.A2);
-                t = 1.57079632679490f - asinf(sqrtf(fminf(fmaxf(hf, 0.0f), 1.0f)));
-            }
-            g = t * t;
-        }
-        return ex2_approx(-e.K * g);
-    }
-
-    __device__ static void norm_add(const Ext &e, const SegReg &sr, int j, int pix, NormAcc &acc) {
-        (void)pix;
-        const float w = weight(e, sr, j);
-        const float y = __fsub_rn(w, acc.c);  // Kahan step
-        const float t = __fadd_rn(acc.s, y);
-        acc.c = __fsub_rn(__fsub_rn(t, acc.s), y);
-        acc.s = t;
-    }
-    __device__ static double norm_value(const NormAcc &acc) { return (double)acc.s - (double)acc.c; }
-
-    __device__ static void deposit_setup(const DiscArgs &a, const DiscHdr &d, const Ext &e, double S,
-                                         Dep &dep) {
-        (void)e;
-        const double F = d.flux * a.f.inv_scale / S;
-        dep.F = (float)F;
-        dep.Flo = (float)(F - (double)dep.F);
-    }
-    // w * F as hi + lo: the product's rounding error (exact, from an FMA) and
-    // w * Flo travel to the lo plane with the atomic's TwoSum error, so a
-    // particle's deposits add up to its flux to ~1e-12, not to FP32 rounding.
-    __device__ static void deposit(const DiscArgs &a, const Ext &e, const Dep &dep, const SegReg &sr,
-                                   int j, int pix) {
-        const float w = weight(e, sr, j);
-        const float p = w * dep.F;
-        const float pe = fmaf(w, dep.Flo, fmaf(w, dep.F, -p));
-        deposit2f(a.acc.hi, a.acc.lo, pix, p, pe);
-    }
-    __device__ static void single(const DiscArgs &a, const DiscHdr &d) {
-        const double vs = d.flux * a.f.inv_scale;
-        const float vh = (float)vs;
-        const float vl = (float)(vs - (double)vh);
-        deposit2f(a.acc.hi, a.acc.lo, d.cpix, vh);
-        if (vl != 0.0f) red_add_f32(a.acc.lo + d.cpix, vl);
-    }
+// One run: pixels pix0 .. pix0+cnt-1 of one ring, in order of increasing
+// azimuth; x(j) = d0h + j*steph is half the azimuth offset of pixel j from
+// the particle.
+struct alignas(16) Run {
+    int pix0, cnt;
+    float A, B;         // hav(theta_r - theta0), sin(theta_r) sin(theta0)
+    float d0h, steph;   // half azimuth offset of pixel 0, half the pixel step
+    float A2, pad;      // hav(theta_r + theta0 - pi): distance to the antipode
 };
 
-constexpr int kBT = 256, kRCH = 512;
-constexpr int kWPB = 8, kRCHW = 64;
+struct Ext {
+    float nK;           // -K
+    int small_h, small_x;
+};
+
+template <int RCH>
+struct CompSmem {
+    Run run[2 * RCH];   // two runs per ring (the second only where it wraps)
+    DiscHdr hdr;
+    Ext ext;
+    double red[32];
+    int cnt_red[32];
+};
+
+__device__ inline void particle_setup(const DiscHdr &d, Ext &e) {
+    e.nK = -(float)(4.0 * 1.4426950408889634 * 0.5 / (0.333 * d.ar * d.ar));
+    double hmax = 1.0;
+    if (!d.allsky) {
+        const double s = sin(0.5 * d.R);
+        hmax = s * s;
+    }
+    e.small_h = hmax < 0.02;
+    const bool caps = d.allsky || d.r_first < d.irmin || d.r_last > d.irmax;
+    int small_x = 0;
+    if (!caps) {
+        const double sr = sin(d.R);
+        if (sr < 0.999 * d.sth0) small_x = (0.5 * asin(sr / d.sth0)) < 0.33;
+    }
+    e.small_x = small_x;
+}
+
+// Stages ring `ring` as run(s) run[0], run[1]; returns its pixel count.
+__device__ inline int make_runs(const DiscArgs &a, const DiscHdr &d, int ring, Run *run) {
+    int lo, cnt;
+    ring_segment_t<true>(a.g, d, ring, lo, cnt);
+    run[0].cnt = 0;
+    run[1].cnt = 0;
+    if (cnt <= 0) return 0;
+    const int start = (int)ring_start(a.g, ring);
+    const int nr = ring_npix(a.g, ring);
+    const double shift = ring_shifted(a.g, ring) ? 0.5 : 0.0;
+    const double step = a.rt.step[ring];
+    const double th = a.rt.theta[ring];
+    const float sa = sinf(0.5f * (float)(th - d.theta0));
+    const float sb = sinf(0.5f * (float)(th + d.theta0 - kPi));
+    const float A = sa * sa, A2 = sb * sb;
+    const float B = (float)(a.rt.st[ring] * d.sth0);
+    const float steph = (float)(0.5 * step);
+    // azimuth of the first pixel relative to the particle, in [-pi, pi)
+    double d0 = ((double)lo + shift) * step - d.phi0;
+    if (d0 < -kPi) d0 += kTwoPi;
+    if (d0 >= kPi) d0 -= kTwoPi;
+    // split where the in-ring index wraps (lo < 0 or lo + cnt > nr)
+    int c0 = cnt, p0 = start + lo;
+    if (lo < 0) {
+        c0 = -lo;
+        p0 = start + lo + nr;
+    } else if (lo + cnt > nr) {
+        c0 = nr - lo;
+    }
+    run[0] = Run{p0, c0, A, B, (float)(0.5 * d0), steph, A2, 0.0f};
+    if (c0 < cnt) {
+        // the rest continues at the ring's first pixel, azimuth continuing
+        run[1] = Run{start, cnt - c0, A, B, (float)(0.5 * (d0 + (double)c0 * step)), steph, A2, 0.0f};
+    }
+    return cnt;
+}
+
+// sin x, |x| <= pi/2, Taylor to x^15 (scalar; the general path)
+__device__ inline float sin_large(float x) {
+    const float x2 = x * x;
+    float p = fmaf(x2, -1.0f / 1307674368000.0f, 1.0f / 6227020800.0f);
+    p = fmaf(x2, p, -1.0f / 39916800.0f);
+    p = fmaf(x2, p, 1.0f / 362880.0f);
+    p = fmaf(x2, p, -1.0f / 5040.0f);
+    p = fmaf(x2, p, 1.0f / 120.0f);
+    p = fmaf(x2, p, -1.0f / 6.0f);
+    p = fmaf(x2, p, 1.0f);
+    return x * p;
+}
+
+// theta^2 / 4 for large discs: asin^2(sqrt h), or beyond 90 degrees via the
+// distance to the antipode (x -+ pi/2 is half the azimuth offset from it).
+__device__ inline float g_general(float h, float x, const Run &r) {
+    float t;
+    if (h <= 0.5f) {
+        t = asinf(sqrtf(fmaxf(h, 0.0f)));
+    } else {
+        const float sf = sin_large(x - copysignf(kHalfPiF, x));
+        const float hf = fmaf(r.B, sf * sf, r.A2);
+        t = kHalfPiF - asinf(sqrtf(fminf(fmaxf(hf, 0.0f), 1.0f)));
+    }
+    return t * t;
+}
+
+// Weights of pixels jj = (j, j + 32) of run r.
+__device__ __forceinline__ float2 weight2(const Ext &e, const Run &r, float2 jj) {
+    const float2 x = fma2(jj, f2(r.steph), f2(r.d0h));
+    const float2 x2 = mul2(x, x);
+    float2 p;
+    if (e.small_x) {
+        p = fma2(x2, f2(-1.0f / 5040.0f), f2(1.0f / 120.0f));
+        p = fma2(x2, p, f2(-1.0f / 6.0f));
+        p = fma2(x2, p, f2(1.0f));
+    } else {
+        p = fma2(x2, f2(-1.0f / 1307674368000.0f), f2(1.0f / 6227020800.0f));
+        p = fma2(x2, p, f2(-1.0f / 39916800.0f));
+        p = fma2(x2, p, f2(1.0f / 362880.0f));
+        p = fma2(x2, p, f2(-1.0f / 5040.0f));
+        p = fma2(x2, p, f2(1.0f / 120.0f));
+        p = fma2(x2, p, f2(-1.0f / 6.0f));
+        p = fma2(x2, p, f2(1.0f));
+    }
+    const float2 sn = mul2(x, p);
+    const float2 h = fma2(f2(r.B), mul2(sn, sn), f2(r.A));
+    float2 g;
+    if (e.small_h) {
+        float2 q = fma2(h, f2(128.0f / 1575.0f), f2(4.0f / 35.0f));
+        q = fma2(h, q, f2(8.0f / 45.0f));
+        q = fma2(h, q, f2(1.0f / 3.0f));
+        q = fma2(h, q, f2(1.0f));
+        g = mul2(h, q);
+    } else {
+        g = make_float2(g_general(h.x, x.x, r), g_general(h.y, x.y, r));
+    }
+    const float2 t = mul2(g, f2(e.nK));
+    return make_float2(ex2_approx(t.x), ex2_approx(t.y));
+}
+
+template <int G>
+struct Grp {
+    static constexpr int kWarps = G / 32;
+    __device__ static void sync() {
+        if (G == 32) __syncwarp(); else __syncthreads();
+    }
+    __device__ static int rank() { return G == 32 ? (threadIdx.x & 31) : (int)threadIdx.x; }
+    __device__ static int warp() { return G == 32 ? 0 : (int)(threadIdx.x >> 5); }
+};
+
+// Stages rings r0 .. r0+n-1 as runs; returns the chunk's pixel count (all
+// threads of the group).
+template <int G, int RCH>
+__device__ inline int build_runs(const DiscArgs &a, CompSmem<RCH> &sm, int r0, int n) {
+    using Gp = Grp<G>;
+    int c = 0;
+    for (int i = Gp::rank(); i < n; i += G) c += make_runs(a, sm.hdr, r0 + i, &sm.run[2 * i]);
+    c = __reduce_add_sync(0xffffffffu, c);
+    if (G > 32) {
+        if ((threadIdx.x & 31) == 0) sm.cnt_red[Gp::warp()] = c;
+        Gp::sync();
+        c = 0;
+        for (int k = 0; k < Gp::kWarps; k++) c += sm.cnt_red[k];
+    }
+    Gp::sync();
+    return c;
+}
+
+// Walks the staged runs: warp w takes runs w, w + warps, ...; lane l handles
+// pixels l and l + 32 of each 64-pixel stretch of a run.  body(run, j, second)
+// gets the first pixel index j and whether j + 32 is inside the run.
+template <int G, int RCH, class Body>
+__device__ inline void run_walk(const CompSmem<RCH> &sm, int n, Body body) {
+    using Gp = Grp<G>;
+    const int lane = threadIdx.x & 31;
+    for (int q = Gp::warp(); q < 2 * n; q += Gp::kWarps) {
+        const Run r = sm.run[q];
+        for (int j = lane; j < r.cnt; j += 64) body(r, j, j + 32 < r.cnt);
+    }
+}
+
+// Renders one particle with a group of G threads (a warp or a block).
+template <int G, int RCH>
+__device__ void render_particle(const DiscArgs &a, CompSmem<RCH> &sm, int pidx) {
+    using Gp = Grp<G>;
+    const int rk = Gp::rank();
+    if (rk == 0) {
+        disc_setup(a.g, a.theta[pidx], a.phi[pidx], a.ar[pidx], a.flux[pidx], a.cpix[pidx], pidx,
+                   sm.hdr);
+        particle_setup(sm.hdr, sm.ext);
+    }
+    Gp::sync();
+    const Ext e = sm.ext;
+    const int r_first = sm.hdr.r_first, r_last = sm.hdr.r_last;
+    const int nring = r_last - r_first + 1;
+    const int nchunk = nring > 0 ? (nring + RCH - 1) / RCH : 0;
+
+    // pass 1: the normalisation, Kahan-compensated per lane (both halves)
+    float2 ks = f2(0.0f), kc = f2(0.0f);
+    long long total = 0;
+    for (int c = 0; c < nchunk; c++) {
+        const int r0 = r_first + c * RCH;
+        const int n = min(RCH, r_last - r0 + 1);
+        total += build_runs<G, RCH>(a, sm, r0, n);
+        run_walk<G, RCH>(sm, n, [&](const Run &r, int j, bool second) {
+            const float jf = (float)j;
+            float2 w = weight2(e, r, make_float2(jf, jf + 32.0f));
+            if (!second) w.y = 0.0f;
+            const float2 y = sub2(w, kc);
+            const float2 t = add2(ks, y);
+            kc = sub2(sub2(t, ks), y);
+            ks = t;
+        });
+        Gp::sync();
+    }
+    double part = ((double)ks.x - (double)kc.x) + ((double)ks.y - (double)kc.y);
+    part = warp_sum(part);
+    double S = part;
+    if (G > 32) {
+        if ((rk & 31) == 0) sm.red[rk >> 5] = part;
+        Gp::sync();
+        S = 0.0;
+        for (int k = 0; k < Gp::kWarps; k++) S += sm.red[k];
+        Gp::sync();
+    }
+    if (total < 2) {  // genmap.cpp:125-128: the whole flux into the centre pixel
+        if (rk == 0) {
+            const double vs = sm.hdr.flux * a.f.inv_scale;
+            const float vh = (float)vs;
+            const float vl = (float)(vs - (double)vh);
+            deposit2f(a.acc.hi, a.acc.lo, sm.hdr.cpix, vh);
+            if (vl != 0.0f) red_add_f32(a.acc.lo + sm.hdr.cpix, vl);
+            atomicAdd((unsigned long long *)(a.ctr + C_DEPOSITS), 1ull);
+        }
+        Gp::sync();
+        return;
+    }
+    if (rk == 0) atomicAdd((unsigned long long *)(a.ctr + C_DEPOSITS), (unsigned long long)total);
+    // flux / norm as a two-float
+    const double Fd = sm.hdr.flux * a.f.inv_scale / S;
+    const float F = (float)Fd, Flo = (float)(Fd - (double)F);
+    float *const hi = a.acc.hi, *const lo = a.acc.lo;
+
+    // pass 2: deposits.  w*F as hi + lo: the product's rounding error (exact,
+    // from an FMA) and w*Flo go to the lo plane with the TwoSum error of the
+    // hi atomic, so a particle's deposits add up to its flux to ~1e-12.
+    for (int c = 0; c < nchunk; c++) {
+        const int r0 = r_first + c * RCH;
+        const int n = min(RCH, r_last - r0 + 1);
+        if (nchunk > 1) build_runs<G, RCH>(a, sm, r0, n);
+        run_walk<G, RCH>(sm, n, [&](const Run &r, int j, bool second) {
+            const float jf = (float)j;
+            const float2 w = weight2(e, r, make_float2(jf, jf + 32.0f));
+            const float2 p = mul2(w, f2(F));
+            const float2 pe = fma2(w, f2(Flo), fma2(w, f2(F), make_float2(-p.x, -p.y)));
+            const int pix = r.pix0 + j;
+            const float a0 = atom_add_f32(hi + pix, p.x);
+            const float a1 = second ? atom_add_f32(hi + pix + 32, p.y) : 0.0f;
+            const float2 av = make_float2(a0, a1);
+            const float2 pv = make_float2(p.x, second ? p.y : 0.0f);
+            const float2 s = add2(av, pv);
+            const float2 bb = sub2(s, av);
+            float2 err = add2(sub2(av, sub2(s, bb)), sub2(pv, bb));
+            err = add2(err, pe);
+            red_add_f32(lo + pix, err.x);
+            if (second) red_add_f32(lo + pix + 32, err.y);
+        });
+        Gp::sync();
+    }
+}
+
+constexpr int kBT = 256, kRCH = 384;   // block kernel: 8 blocks x 24.6 KB of runs per SM
+constexpr int kWPB = 8, kRCHW = 64;    // warp kernel
+
+// One 256-thread block per large disc, persistent over the block-class queue
+// (largest discs first, claimed dynamically).  Eight resident blocks per SM
+// are asked of the compiler: the kernel is latency bound (returned atomics),
+// and full occupancy measured fastest.
+__global__ void __launch_bounds__(kBT, 8) k_comp_block(DiscArgs a) {
+    __shared__ CompSmem<kRCH> sm;
+    __shared__ int s_q;
+    const long long nblk = a.ctr[C_ADD_BLOCK];
+    for (;;) {
+        if (threadIdx.x == 0) s_q = (int)atomicAdd((unsigned long long *)(a.ctr + C_QNEXT_BLOCK), 1ull);
+        __syncthreads();
+        const int q = s_q;
+        __syncthreads();
+        if (q >= nblk) break;
+        render_particle<kBT, kRCH>(a, sm, a.queue[q]);
+    }
+}
+
+// One warp per small disc over the warp-class queue (after the block class).
+__global__ void __launch_bounds__(kWPB * 32) k_comp_warp(DiscArgs a) {
+    __shared__ CompSmem<kRCHW> sm[kWPB];
+    const long long nblk = a.ctr[C_ADD_BLOCK];
+    const long long ndisc = a.ctr[C_ADD_DISC];
+    const int w = threadIdx.x >> 5;
+    const long long gw = (long long)blockIdx.x * kWPB + w;
+    const long long nw = (long long)gridDim.x * kWPB;
+    for (long long q = nblk + gw; q < ndisc; q += nw) render_particle<32, kRCHW>(a, sm[w], a.queue[q]);
+}
 
 }  // namespace
 
 cudaError_t launch_disc_comp(const DiscArgs &a, int num_sms, int blocks_per_sm, cudaStream_t s,
                              cudaEvent_t mid) {
     int occ = 0;
-    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-        &occ, k_disc_block<CompForm, kBT, kRCH>, kBT, 0);
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_comp_block, kBT, 0);
     if (e != cudaSuccess) return e;
     int bps = blocks_per_sm > 0 ? min(blocks_per_sm, occ) : occ;
     if (bps < 1) bps = 1;
-    k_disc_block<CompForm, kBT, kRCH><<<num_sms * bps, kBT, 0, s>>>(a);
-    e = cudaGetLastError();
-    if (e != cudaSuccess) return e;
+    k_comp_block<<<num_sms * bps, kBT, 0, s>>>(a);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
     if (mid && (e = cudaEventRecord(mid, s)) != cudaSuccess) return e;
     int occw = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occw, k_disc_warp<CompForm, kWPB, kRCHW>,
-                                                      kWPB * 32, 0);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occw, k_comp_warp, kWPB * 32, 0);
     if (e != cudaSuccess) return e;
     if (occw < 1) occw = 1;
-    k_disc_warp<CompForm, kWPB, kRCHW><<<num_sms * occw, kWPB * 32, 0, s>>>(a);
+    k_comp_warp<<<num_sms * occw, kWPB * 32, 0, s>>>(a);
     return cudaGetLastError();
 }
 
