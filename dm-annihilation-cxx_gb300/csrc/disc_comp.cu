@@ -14,7 +14,8 @@
 // angles.  Beyond 90 degrees (hav > 1/2) the distance is taken to the
 // particle's antipode, where asin(sqrt(h)) would lose precision.
 //
-// Normalisation: a Kahan-compensated FP32 sum per thread, reduced in FP64.
+// Normalisation: a compensated FP32 sum per thread (offset so that Fast2Sum
+// captures every rounding error exactly), reduced in FP64.
 // Deposits: two FP32 planes (hi, lo); the hi atomic returns the old value, so
 // the exact TwoSum error of each addition -- plus the product's own rounding
 // error and the low part of flux/norm -- goes to the lo plane.
@@ -77,6 +78,7 @@ struct CompSmem {
     Ext ext;
     double red[32];
     int cnt_red[32];
+    int next_run;       // runs claimed so far in the current pass (block groups)
 };
 
 __device__ inline void particle_setup(const DiscHdr &d, Ext &e) {
@@ -222,14 +224,26 @@ __device__ inline int build_runs(const DiscArgs &a, CompSmem<RCH> &sm, int r0, i
     return c;
 }
 
-// Walks the staged runs: warp w takes runs w, w + warps, ...; lane l handles
-// pixels l and l + 32 of each 64-pixel stretch of a run.  body(run, j, second)
-// gets the first pixel index j and whether j + 32 is inside the run.
+// Walks the staged runs; lane l handles pixels l and l + 32 of each 64-pixel
+// stretch of a run.  body(run, j, second) gets the first pixel index j and
+// whether j + 32 is inside the run.  In a block, warps claim runs one at a
+// time from a shared counter (reset by the caller), so no warp waits at the
+// next barrier for more than about one run: ring runs differ a lot in length.
 template <int G, int RCH, class Body>
-__device__ inline void run_walk(const CompSmem<RCH> &sm, int n, Body body) {
-    using Gp = Grp<G>;
+__device__ inline void run_walk(CompSmem<RCH> &sm, int n, Body body) {
     const int lane = threadIdx.x & 31;
-    for (int q = Gp::warp(); q < 2 * n; q += Gp::kWarps) {
+    if (G == 32) {
+        for (int q = 0; q < 2 * n; q++) {
+            const Run r = sm.run[q];
+            for (int j = lane; j < r.cnt; j += 64) body(r, j, j + 32 < r.cnt);
+        }
+        return;
+    }
+    for (;;) {
+        int q = 0;
+        if (lane == 0) q = atomicAdd(&sm.next_run, 1);
+        q = __shfl_sync(0xffffffffu, q, 0);
+        if (q >= 2 * n) break;
         const Run r = sm.run[q];
         for (int j = lane; j < r.cnt; j += 64) body(r, j, j + 32 < r.cnt);
     }
@@ -251,25 +265,34 @@ __device__ void render_particle(const DiscArgs &a, CompSmem<RCH> &sm, int pidx) 
     const int nring = r_last - r_first + 1;
     const int nchunk = nring > 0 ? (nring + RCH - 1) / RCH : 0;
 
-    // pass 1: the normalisation, Kahan-compensated per lane (both halves)
-    float2 ks = f2(0.0f), kc = f2(0.0f);
+    // pass 1: the normalisation, a compensated sum per lane (both halves).
+    // The sums start at 1 and every weight is <= 1, so the running sum always
+    // dominates the addend and Fast2Sum gives each step's rounding error
+    // exactly; the errors are summed apart (not fed back into the next addend,
+    // where Kahan's subtraction would round them away again).  The result is
+    // independent of the order in which lanes meet the weights to ~1e-12.
+    // The offset is removed in FP64.
+    float2 ks = f2(1.0f), kc = f2(0.0f);
     long long total = 0;
     for (int c = 0; c < nchunk; c++) {
         const int r0 = r_first + c * RCH;
         const int n = min(RCH, r_last - r0 + 1);
         total += build_runs<G, RCH>(a, sm, r0, n);
+        if (G > 32) {
+            if (rk == 0) sm.next_run = 0;
+            Gp::sync();
+        }
         run_walk<G, RCH>(sm, n, [&](const Run &r, int j, bool second) {
             const float jf = (float)j;
             float2 w = weight2(e, r, make_float2(jf, jf + 32.0f));
             if (!second) w.y = 0.0f;
-            const float2 y = sub2(w, kc);
-            const float2 t = add2(ks, y);
-            kc = sub2(sub2(t, ks), y);
+            const float2 t = add2(ks, w);
+            kc = add2(kc, sub2(w, sub2(t, ks)));
             ks = t;
         });
         Gp::sync();
     }
-    double part = ((double)ks.x - (double)kc.x) + ((double)ks.y - (double)kc.y);
+    double part = (((double)ks.x - 1.0) + (double)kc.x) + (((double)ks.y - 1.0) + (double)kc.y);
     part = warp_sum(part);
     double S = part;
     if (G > 32) {
@@ -304,6 +327,10 @@ __device__ void render_particle(const DiscArgs &a, CompSmem<RCH> &sm, int pidx) 
         const int r0 = r_first + c * RCH;
         const int n = min(RCH, r_last - r0 + 1);
         if (nchunk > 1) build_runs<G, RCH>(a, sm, r0, n);
+        if (G > 32) {
+            if (rk == 0) sm.next_run = 0;
+            Gp::sync();
+        }
         run_walk<G, RCH>(sm, n, [&](const Run &r, int j, bool second) {
             const float jf = (float)j;
             const float2 w = weight2(e, r, make_float2(jf, jf + 32.0f));
