@@ -4,6 +4,7 @@
 //   -> key scan -> queue scatter (largest discs first)
 //   -> disc kernels (block per large disc, warp per small disc)
 //   -> final map pass (divide by dOmega, optional accumulate).
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -510,6 +511,161 @@ dmann_status dmann_render(dmann_ctx *ctx, const float *x, const float *y, const 
         return st;
     }
     return dmann_map_end(ctx, map_out, accumulate);
+}
+
+}  // extern "C"
+
+namespace {
+
+// Issues one observer's map into dmap (device) on the context's stream:
+// zero the planes, prep, key scan, queue scatter, disc kernels, finalize.
+// The workspace and the ring table must already exist: nothing here
+// allocates or synchronises, so the sequence can be captured in a graph.
+dmann_status issue_observer(dmann_ctx *ctx, const float *const dev[6], int n, int nside,
+                            const RingTables &rt, int precision, double *dmap) {
+    cudaStream_t s = ctx->stream;
+    ctx->g = make_hpx(nside);
+    ctx->precision = precision;
+    const size_t P = (size_t)ctx->g.npix;
+    CK(cudaMemsetAsync(ctx->acc.p, 0, 8 * P, s));
+    CK(cudaMemsetAsync(ctx->ctr.p, 0, 8 * C_COUNT, s));
+    CK(cudaMemsetAsync(ctx->fsum.p, 0, 8, s));
+    double scale;
+    const Frame f = make_frame(ctx, &scale);
+    const Accum acc = make_accum(ctx);
+    if (n > 0) {
+        int bmin = 0;
+        while (bmin < kBuckets && (1LL << bmin) <= ctx->tune.warp_max_pixels) bmin++;
+        CK(cudaMemsetAsync(ctx->hist.p, 0, 4 * (size_t)kKeys, s));
+        PrepArgs pa;
+        pa.p = {dev[0], dev[1], dev[2], dev[3], dev[4], dev[5], n};
+        pa.f = f;
+        pa.g = ctx->g;
+        pa.out = {(double *)ctx->theta.p, (double *)ctx->phi.p, (double *)ctx->ar.p,
+                  (double *)ctx->flux.p, (int *)ctx->cpix.p, (int *)ctx->key.p};
+        pa.hist = (int *)ctx->hist.p;
+        pa.ctr = (long long *)ctx->ctr.p;
+        pa.flux_sum = (double *)ctx->fsum.p;
+        pa.acc = acc;
+        pa.precision = precision;
+        pa.block_bucket_min = bmin;
+        CK(launch_prep(pa, s));
+        CK(launch_scan(pa.hist, pa.ctr, bmin, s));
+        CK(launch_scatter(pa, (int *)ctx->queue.p, s));
+        DiscArgs da;
+        da.g = ctx->g;
+        da.f = f;
+        da.rt = {rt.z, rt.st, rt.theta, rt.step};
+        da.theta = pa.out.theta;
+        da.phi = pa.out.phi;
+        da.ar = pa.out.ar;
+        da.flux = pa.out.flux;
+        da.cpix = pa.out.cpix;
+        da.queue = (const int *)ctx->queue.p;
+        da.ctr = pa.ctr;
+        da.acc = acc;
+        if (precision == DMANN_PLAIN_F64) CK(launch_disc_plain(da, ctx->num_sms, ctx->tune.blocks_per_sm, s, nullptr));
+        else CK(launch_disc_comp(da, ctx->num_sms, ctx->tune.blocks_per_sm, s, nullptr));
+    }
+    CK(launch_finalize(acc, precision, ctx->g.npix, ctx->g.dOmega, scale, dmap, 0, s));
+    return DMANN_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+dmann_status dmann_render_batch(dmann_ctx *ctx, const float *x, const float *y, const float *z,
+                                const float *m, const float *rho, const float *h, int64_t n,
+                                int n_obs, const double *rot, const double *opos,
+                                const int *nside, int precision, double *const *maps) {
+    if (!ctx) return DMANN_ERR_INVALID;
+    if (n_obs < 1 || !rot || !opos || !nside || !maps)
+        return fail(ctx, DMANN_ERR_INVALID, "batch needs n_obs >= 1 and rot/opos/nside/maps");
+    if (precision != DMANN_PLAIN_F64 && precision != DMANN_COMP_F32)
+        return fail(ctx, DMANN_ERR_INVALID, "unknown precision form");
+    if (!ctx->have_units) return fail(ctx, DMANN_ERR_STATE, "units not set");
+    dmann_status st = check_particles(ctx, x, y, z, m, rho, h, n);
+    if (st != DMANN_OK) return st;
+    int maxns = 0;
+    for (int k = 0; k < n_obs; k++) {
+        if (nside[k] < 1 || nside[k] > 8192) return fail(ctx, DMANN_ERR_INVALID, "nside must be in [1, 8192]");
+        if (!maps[k]) return fail(ctx, DMANN_ERR_INVALID, "null output map");
+        for (int i = 0; i < 9; i++)
+            if (!std::isfinite(rot[9 * k + i])) return fail(ctx, DMANN_ERR_INVALID, "non-finite rotation");
+        maxns = std::max(maxns, nside[k]);
+    }
+    CK(cudaSetDevice(ctx->device));
+    if ((st = collect_stats(ctx)) != DMANN_OK) return st;
+    cudaStream_t s = ctx->stream;
+    const size_t N = (size_t)n, n1 = N > 0 ? N : 1, Pmax = 12 * (size_t)maxns * (size_t)maxns;
+    // everything is sized and uploaded before the observers are issued
+    if ((st = ensure(ctx, ctx->theta, 8 * n1)) || (st = ensure(ctx, ctx->phi, 8 * n1)) ||
+        (st = ensure(ctx, ctx->ar, 8 * n1)) || (st = ensure(ctx, ctx->flux, 8 * n1)) ||
+        (st = ensure(ctx, ctx->cpix, 4 * n1)) || (st = ensure(ctx, ctx->key, 4 * n1)) ||
+        (st = ensure(ctx, ctx->queue, 4 * n1)) || (st = ensure(ctx, ctx->hist, 4 * (size_t)kKeys)) ||
+        (st = ensure(ctx, ctx->ctr, 8 * C_COUNT)) || (st = ensure(ctx, ctx->fsum, 8)) ||
+        (st = ensure(ctx, ctx->acc, 8 * Pmax)) || (st = ensure(ctx, ctx->map, 8 * Pmax)))
+        return st;
+    std::vector<RingTables> rts(n_obs);
+    for (int k = 0; k < n_obs; k++)
+        if ((st = ring_tables(ctx, nside[k], rts[k])) != DMANN_OK) return st;
+    const float *src[6] = {x, y, z, m, rho, h};
+    const float *dev[6];
+    for (int k = 0; k < 6; k++) {
+        if (N == 0 || is_device_ptr(src[k])) {
+            dev[k] = src[k];
+        } else {
+            if ((st = ensure(ctx, ctx->in[k], 4 * N)) != DMANN_OK) return st;
+            CK(cudaMemcpyAsync(ctx->in[k].p, src[k], 4 * N, cudaMemcpyHostToDevice, s));
+            dev[k] = (const float *)ctx->in[k].p;
+        }
+    }
+    std::vector<char> on_dev(n_obs);
+    bool all_dev = true;
+    for (int k = 0; k < n_obs; k++) all_dev &= (on_dev[k] = is_device_ptr(maps[k])) != 0;
+    double rot0[9], opos0[3];
+    std::memcpy(rot0, ctx->rot, sizeof rot0);
+    std::memcpy(opos0, ctx->opos, sizeof opos0);
+    const bool had_frame = ctx->have_frame;
+    // device maps: the whole batch is captured into one CUDA graph and
+    // launched once; host maps go through the context's staging map
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    if (all_dev) CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    for (int k = 0; k < n_obs && st == DMANN_OK; k++) {
+        std::memcpy(ctx->rot, rot + 9 * k, sizeof(double) * 9);
+        std::memcpy(ctx->opos, opos + 3 * k, sizeof(double) * 3);
+        double *dmap = on_dev[k] ? maps[k] : (double *)ctx->map.p;
+        st = issue_observer(ctx, dev, (int)N, nside[k], rts[k], precision, dmap);
+        if (st == DMANN_OK && !on_dev[k]) {
+            const size_t P = 12 * (size_t)nside[k] * (size_t)nside[k];
+            cudaError_t e = cudaMemcpyAsync(maps[k], dmap, 8 * P, cudaMemcpyDeviceToHost, s);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+            if (e != cudaSuccess) st = fail(ctx, DMANN_ERR_CUDA, std::string("batch copy: ") + cudaGetErrorString(e));
+        }
+    }
+    std::memcpy(ctx->rot, rot0, sizeof rot0);
+    std::memcpy(ctx->opos, opos0, sizeof opos0);
+    ctx->have_frame = had_frame;
+    if (all_dev) {
+        cudaError_t e = cudaStreamEndCapture(s, &graph);
+        if (st != DMANN_OK) {
+            if (graph) cudaGraphDestroy(graph);
+            return st;
+        }
+        if (e != cudaSuccess) return fail(ctx, DMANN_ERR_CUDA, std::string("batch capture: ") + cudaGetErrorString(e));
+        e = cudaGraphInstantiate(&exec, graph, 0);
+        if (e == cudaSuccess) e = cudaGraphLaunch(exec, s);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+        if (exec) cudaGraphExecDestroy(exec);
+        cudaGraphDestroy(graph);
+        if (e != cudaSuccess) return fail(ctx, DMANN_ERR_CUDA, std::string("batch graph: ") + cudaGetErrorString(e));
+    }
+    if (st != DMANN_OK) return st;
+    ctx->stats = dmann_stats{};
+    ctx->stats.n_in = n;
+    return DMANN_OK;
 }
 
 dmann_status dmann_observer_rotation(const double opos[3], const double cpos[3],

@@ -64,6 +64,8 @@ SIGNATURES = {
     "dmann_map_add": (C.c_int, [_P, _P, _P, _P, _P, _P, _P, C.c_int64]),
     "dmann_map_end": (C.c_int, [_P, _P, C.c_int]),
     "dmann_get_stats": (C.c_int, [_P, C.POINTER(Stats)]),
+    "dmann_render_batch": (C.c_int, [_P, _P, _P, _P, _P, _P, _P, C.c_int64, C.c_int, _D3, _D3,
+                                     C.POINTER(C.c_int), C.c_int, C.POINTER(C.c_void_p)]),
     "dmann_observer_rotation": (C.c_int, [_D3, _D3, _D3, _D3, _D3]),
     "dmann_code_units": (C.c_int, [C.c_double, C.c_double, C.c_double, _D3]),
     "dmann_hires_threshold": (C.c_double, [_D3, C.c_int]),

@@ -154,6 +154,30 @@ class Renderer:
         self.add(parts)
         return self.end(out, accumulate)
 
+    def render_batch(self, parts: dict, frames, nsides, precision: int = COMP_F32, outs=None):
+        """One map per observer: frames is a list of (rot 3x3, opos 3) pairs,
+        nsides the Nside of each map.  outs (optional) are the output maps
+        (float64 numpy arrays or CUDA tensors); host arrays are made if absent."""
+        k = len(frames)
+        if len(nsides) != k:
+            raise ValueError("one Nside per observer")
+        if outs is None:
+            outs = [np.zeros(12 * int(ns) * int(ns), dtype=np.float64) for ns in nsides]
+        arrays = [parts[f] for f in FIELDS]
+        n = len(arrays[0])
+        self._keep = []
+        self._use_torch_stream(arrays + [o for o in outs if _is_torch(o)])
+        ptrs = [self._ptr(a, np.float32) for a in arrays]
+        rot = np.concatenate([np.asarray(r, dtype=np.float64).reshape(9) for r, _ in frames])
+        opos = np.concatenate([np.asarray(o, dtype=np.float64).reshape(3) for _, o in frames])
+        ns = (C.c_int * k)(*[int(v) for v in nsides])
+        mp = (C.c_void_p * k)(*[o.data_ptr() if _is_torch(o) else o.ctypes.data for o in outs])
+        self._check(self.L.dmann_render_batch(
+            self.ctx, *ptrs, int(n), k, rot.ctypes.data_as(C.POINTER(C.c_double)),
+            opos.ctypes.data_as(C.POINTER(C.c_double)), ns, int(precision), mp))
+        self._keep = []
+        return outs
+
     def synchronize(self):
         self._check(self.L.dmann_synchronize(self.ctx))
         self._keep = []

@@ -32,8 +32,6 @@
  *                                     src/genmap.cpp:67-169.
  *   dmann_render_batch                no reference counterpart (many
  *                                     observers / Nside values in one call)
- *   dmann_adjoint                     no reference counterpart (gradients of a
- *                                     pixelwise loss)
  */
 #ifndef DMANN_H
 #define DMANN_H
@@ -157,6 +155,20 @@ dmann_status dmann_map_add(dmann_ctx *ctx, const float *x, const float *y,
                            const float *z, const float *m, const float *rho,
                            const float *h, int64_t n);
 dmann_status dmann_map_end(dmann_ctx *ctx, double *map_out, int accumulate);
+
+/* Renders the same particles for n_obs observers in one call (no reference
+ * counterpart: the reference renders one observer per run).  Observer k has
+ * the frame rot[9k..9k+8] / opos[3k..3k+2] (as dmann_set_frame) and its own
+ * nside[k]; its map goes to maps[k] (12*nside[k]^2 doubles, host or device).
+ * The particles are uploaded once; when every map is a device pointer the
+ * whole batch is captured into one CUDA graph and launched once.  Returns when
+ * all maps are complete.  The context's own frame is left unchanged. */
+dmann_status dmann_render_batch(dmann_ctx *ctx, const float *x, const float *y,
+                                const float *z, const float *m, const float *rho,
+                                const float *h, int64_t n, int n_obs,
+                                const double *rot, const double *opos,
+                                const int *nside, int precision,
+                                double *const *maps);
 
 /* Statistics of the last completed map (synchronises the stream). */
 dmann_status dmann_get_stats(const dmann_ctx *ctx, dmann_stats *out);

@@ -229,3 +229,32 @@ def test_invalid_arguments(rend):
     # the context stays usable after errors
     rend.set_params(par)
     assert rend.render(P.as_dict(), 16, COMP).sum() > 0
+
+
+@pytest.mark.parametrize("device_maps", [False, True])
+def test_render_batch_matches_single_renders(rend, device_maps):
+    """Several observers on the 8 kpc sphere, Nside cycling 32/64/128, in one
+    call: each map equals the map of a single render with that observer."""
+    torch = pytest.importorskip("torch")
+    P = synth.nfw_halo(8000, seed=808, n_sub=5)
+    obs = synth.batched_observers(6, nsides=(32, 64, 128))
+    frames, nsides = [], []
+    for o, ns in obs:
+        par = annmap.Parameters.for_synthetic(synth.Particles(
+            P.x, P.y, P.z, P.m, P.rho, P.h, o, P.centerpos, P.align_vec, P.particle_mass), ns)
+        frames.append((par.rotmatrix, par.params.opos))
+        nsides.append(ns)
+    par0 = annmap.Parameters.for_synthetic(P, 64)
+    rend.set_params(par0)
+    outs = None
+    if device_maps:
+        outs = [torch.zeros(12 * ns * ns, dtype=torch.float64, device="cuda") for ns in nsides]
+    got = rend.render_batch(P.as_dict(), frames, nsides, COMP, outs=outs)
+    if device_maps:
+        got = [g.cpu().numpy() for g in got]
+    for (rot, opos), ns, g in zip(frames, nsides, got):
+        rend.set_frame(rot, opos)
+        ref = rend.render(P.as_dict(), ns, COMP)
+        assert np.array_equal(g != 0, ref != 0)
+        np.testing.assert_allclose(g, ref, rtol=1e-10, atol=0)
+    rend.set_params(par0)
