@@ -42,16 +42,22 @@ struct dmann_ctx {
     bool have_frame = false, have_units = false;
     double rot[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
     double opos[3] = {0, 0, 0};
+    // halo centre and alignment of the last dmann_set_observer (the adjoint
+    // differentiates the rotation through them); unset after dmann_set_frame
+    bool have_geom = false;
+    double cpos[3] = {0, 0, 0}, align[3] = {0, 0, 0};
     double unit_factor = 1.0, hires = INFINITY;
     int flux_model = DMANN_FLUX_ANN_NOSOM;
     dmann_tuning tune{};
     std::map<int, RingTables> rings;
     // workspace
     DevBuf in[6], theta, phi, ar, flux, cpix, key, queue, hist, ctr, fsum, acc, map;
+    DevBuf cls, oacc, grad;   // the adjoint's class array, observer sums, staged gradient
     dmann_stats stats{};
     bool stats_pending = false;
-    long long *h_ctr = nullptr;   // pinned: C_COUNT counters + the flux sum
+    long long *h_ctr = nullptr;   // pinned: C_COUNT counters, the flux sum, 12 adjoint sums
     double *h_fsum = nullptr;
+    double *h_oacc = nullptr;
     // the map being accumulated (dmann_map_begin .. dmann_map_end)
     Hpx g{};
     RingTables rt;
@@ -217,12 +223,13 @@ dmann_status dmann_create(dmann_ctx **out, int device) {
         cudaEventCreate(&ctx->ev0) != cudaSuccess || cudaEventCreate(&ctx->ev1) != cudaSuccess ||
         cudaEventCreate(&ctx->evd0) != cudaSuccess || cudaEventCreate(&ctx->evd1) != cudaSuccess ||
         cudaEventCreate(&ctx->evdm) != cudaSuccess ||
-        cudaHostAlloc((void **)&ctx->h_ctr, 8 * (C_COUNT + 1), cudaHostAllocDefault) != cudaSuccess) {
+        cudaHostAlloc((void **)&ctx->h_ctr, 8 * (C_COUNT + 1 + 12), cudaHostAllocDefault) != cudaSuccess) {
         cudaGetLastError();
         delete ctx;
         return DMANN_ERR_CUDA;
     }
     ctx->h_fsum = (double *)(ctx->h_ctr + C_COUNT);
+    ctx->h_oacc = (double *)(ctx->h_ctr + C_COUNT + 1);
     ctx->stream = ctx->own;
     ctx->tune.warp_max_pixels = 1024;
     ctx->tune.block_threads = 256;
@@ -238,7 +245,8 @@ void dmann_destroy(dmann_ctx *ctx) {
     cudaStreamSynchronize(ctx->stream);
     DevBuf *bufs[] = {&ctx->in[0], &ctx->in[1], &ctx->in[2], &ctx->in[3], &ctx->in[4], &ctx->in[5],
                       &ctx->theta, &ctx->phi, &ctx->ar, &ctx->flux, &ctx->cpix, &ctx->key,
-                      &ctx->queue, &ctx->hist, &ctx->ctr, &ctx->fsum, &ctx->acc, &ctx->map};
+                      &ctx->queue, &ctx->hist, &ctx->ctr, &ctx->fsum, &ctx->acc, &ctx->map,
+                      &ctx->cls, &ctx->oacc, &ctx->grad};
     for (DevBuf *b : bufs)
         if (b->p) cudaFree(b->p);
     for (auto &kv : ctx->rings) {
@@ -280,6 +288,9 @@ dmann_status dmann_set_observer(dmann_ctx *ctx, const double opos[3], const doub
         return fail(ctx, DMANN_ERR_INVALID, "observer position equals the halo centre");
     std::memcpy(ctx->rot, rot, sizeof rot);
     std::memcpy(ctx->opos, opos, sizeof(double) * 3);
+    std::memcpy(ctx->cpos, cpos, sizeof(double) * 3);
+    std::memcpy(ctx->align, align, sizeof(double) * 3);
+    ctx->have_geom = true;
     ctx->have_frame = true;
     return DMANN_OK;
 }
@@ -290,6 +301,7 @@ dmann_status dmann_set_frame(dmann_ctx *ctx, const double rot[9], const double o
         if (!std::isfinite(rot[i])) return fail(ctx, DMANN_ERR_INVALID, "non-finite rotation");
     std::memcpy(ctx->rot, rot, sizeof(double) * 9);
     std::memcpy(ctx->opos, opos, sizeof(double) * 3);
+    ctx->have_geom = false;
     ctx->have_frame = true;
     return DMANN_OK;
 }
@@ -443,6 +455,7 @@ dmann_status dmann_map_add(dmann_ctx *ctx, const float *x, const float *y, const
     pa.acc = acc;
     pa.precision = ctx->precision;
     pa.block_bucket_min = bmin;
+    pa.deposit_singles = 1;
     CK(launch_prep(pa, s));
     CK(launch_scan(pa.hist, pa.ctr, bmin, s));
     CK(launch_scatter(pa, (int *)ctx->queue.p, s));
@@ -549,6 +562,7 @@ dmann_status issue_observer(dmann_ctx *ctx, const float *const dev[6], int n, in
         pa.acc = acc;
         pa.precision = precision;
         pa.block_bucket_min = bmin;
+        pa.deposit_singles = 1;
         CK(launch_prep(pa, s));
         CK(launch_scan(pa.hist, pa.ctr, bmin, s));
         CK(launch_scatter(pa, (int *)ctx->queue.p, s));
@@ -627,7 +641,7 @@ dmann_status dmann_render_batch(dmann_ctx *ctx, const float *x, const float *y, 
     double rot0[9], opos0[3];
     std::memcpy(rot0, ctx->rot, sizeof rot0);
     std::memcpy(opos0, ctx->opos, sizeof opos0);
-    const bool had_frame = ctx->have_frame;
+    const bool had_frame = ctx->have_frame, had_geom = ctx->have_geom;
     // device maps: the whole batch is captured into one CUDA graph and
     // launched once; host maps go through the context's staging map
     cudaGraph_t graph = nullptr;
@@ -648,6 +662,7 @@ dmann_status dmann_render_batch(dmann_ctx *ctx, const float *x, const float *y, 
     std::memcpy(ctx->rot, rot0, sizeof rot0);
     std::memcpy(ctx->opos, opos0, sizeof opos0);
     ctx->have_frame = had_frame;
+    ctx->have_geom = had_geom;
     if (all_dev) {
         cudaError_t e = cudaStreamEndCapture(s, &graph);
         if (st != DMANN_OK) {
@@ -668,6 +683,121 @@ dmann_status dmann_render_batch(dmann_ctx *ctx, const float *x, const float *y, 
     return DMANN_OK;
 }
 
+dmann_status dmann_adjoint(dmann_ctx *ctx, const float *x, const float *y, const float *z,
+                           const float *m, const float *rho, const float *h, int64_t n, int nside,
+                           const double *grad_map, double *grad, double grad_opos[3]) {
+    if (!ctx) return DMANN_ERR_INVALID;
+    if (!grad_map || !grad || !grad_opos)
+        return fail(ctx, DMANN_ERR_INVALID, "grad_map, grad and grad_opos are required");
+    if (nside < 1 || nside > 8192) return fail(ctx, DMANN_ERR_INVALID, "nside must be in [1, 8192]");
+    if (!ctx->have_frame) return fail(ctx, DMANN_ERR_STATE, "observer frame not set");
+    if (!ctx->have_units) return fail(ctx, DMANN_ERR_STATE, "units not set");
+    dmann_status st = check_particles(ctx, x, y, z, m, rho, h, n);
+    if (st != DMANN_OK) return st;
+    CK(cudaSetDevice(ctx->device));
+    if ((st = collect_stats(ctx)) != DMANN_OK) return st;
+    cudaStream_t s = ctx->stream;
+    const Hpx g = make_hpx(nside);
+    const size_t N = (size_t)n, n1 = N > 0 ? N : 1, P = (size_t)g.npix;
+    RingTables rt;
+    if ((st = ring_tables(ctx, nside, rt)) != DMANN_OK) return st;
+    if ((st = ensure(ctx, ctx->theta, 8 * n1)) || (st = ensure(ctx, ctx->phi, 8 * n1)) ||
+        (st = ensure(ctx, ctx->ar, 8 * n1)) || (st = ensure(ctx, ctx->flux, 8 * n1)) ||
+        (st = ensure(ctx, ctx->cpix, 4 * n1)) || (st = ensure(ctx, ctx->key, 4 * n1)) ||
+        (st = ensure(ctx, ctx->queue, 4 * n1)) || (st = ensure(ctx, ctx->cls, n1)) ||
+        (st = ensure(ctx, ctx->hist, 4 * (size_t)kKeys)) || (st = ensure(ctx, ctx->ctr, 8 * C_COUNT)) ||
+        (st = ensure(ctx, ctx->fsum, 8)) || (st = ensure(ctx, ctx->oacc, 8 * 12)))
+        return st;
+    const float *src[6] = {x, y, z, m, rho, h};
+    const float *dev[6];
+    for (int k = 0; k < 6; k++) {
+        if (N == 0 || is_device_ptr(src[k])) {
+            dev[k] = src[k];
+        } else {
+            if ((st = ensure(ctx, ctx->in[k], 4 * N)) != DMANN_OK) return st;
+            CK(cudaMemcpyAsync(ctx->in[k].p, src[k], 4 * N, cudaMemcpyHostToDevice, s));
+            dev[k] = (const float *)ctx->in[k].p;
+        }
+    }
+    const double *dgmap = grad_map;
+    if (!is_device_ptr(grad_map)) {
+        if ((st = ensure(ctx, ctx->map, 8 * P)) != DMANN_OK) return st;
+        CK(cudaMemcpyAsync(ctx->map.p, grad_map, 8 * P, cudaMemcpyHostToDevice, s));
+        dgmap = (const double *)ctx->map.p;
+    }
+    const bool grad_dev = is_device_ptr(grad);
+    double *dgrad = grad;
+    if (!grad_dev) {
+        if ((st = ensure(ctx, ctx->grad, 48 * n1)) != DMANN_OK) return st;
+        dgrad = (double *)ctx->grad.p;
+    }
+    double scale;
+    const Frame f = make_frame(ctx, &scale);
+    int bmin = 0;
+    while (bmin < kBuckets && (1LL << bmin) <= ctx->tune.warp_max_pixels) bmin++;
+    CK(cudaEventRecord(ctx->ev0, s));
+    CK(cudaMemsetAsync(ctx->ctr.p, 0, 8 * C_COUNT, s));
+    CK(cudaMemsetAsync(ctx->fsum.p, 0, 8, s));
+    CK(cudaMemsetAsync(ctx->oacc.p, 0, 8 * 12, s));
+    CK(cudaMemsetAsync(ctx->hist.p, 0, 4 * (size_t)kKeys, s));
+    PrepArgs pa;
+    pa.p = {dev[0], dev[1], dev[2], dev[3], dev[4], dev[5], (int)N};
+    pa.f = f;
+    pa.g = g;
+    pa.out = {(double *)ctx->theta.p, (double *)ctx->phi.p, (double *)ctx->ar.p,
+              (double *)ctx->flux.p, (int *)ctx->cpix.p, (int *)ctx->key.p,
+              (signed char *)ctx->cls.p};
+    pa.hist = (int *)ctx->hist.p;
+    pa.ctr = (long long *)ctx->ctr.p;
+    pa.flux_sum = (double *)ctx->fsum.p;
+    pa.acc = Accum{nullptr, nullptr, nullptr};
+    pa.precision = DMANN_PLAIN_F64;
+    pa.block_bucket_min = bmin;
+    pa.deposit_singles = 0;
+    CK(launch_prep(pa, s));
+    CK(launch_scan(pa.hist, pa.ctr, bmin, s));
+    CK(launch_scatter(pa, (int *)ctx->queue.p, s));
+    DiscArgs da;
+    da.g = g;
+    da.f = f;
+    da.rt = {rt.z, rt.st, rt.theta, rt.step};
+    da.theta = pa.out.theta;
+    da.phi = pa.out.phi;
+    da.ar = pa.out.ar;
+    da.flux = pa.out.flux;
+    da.cpix = pa.out.cpix;
+    da.queue = (const int *)ctx->queue.p;
+    da.ctr = pa.ctr;
+    da.acc = pa.acc;
+    CK(cudaEventRecord(ctx->evd0, s));
+    CK(launch_adjoint(da, pa.p, pa.out.cls, dgmap, dgrad, (double *)ctx->oacc.p, ctx->num_sms, s));
+    CK(cudaEventRecord(ctx->evd1, s));
+    CK(cudaEventRecord(ctx->evdm, s));
+    CK(cudaEventRecord(ctx->ev1, s));
+    if (!grad_dev && N > 0) CK(cudaMemcpyAsync(grad, dgrad, 48 * N, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(ctx->h_ctr, ctx->ctr.p, 8 * C_COUNT, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(ctx->h_fsum, ctx->fsum.p, 8, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(ctx->h_oacc, ctx->oacc.p, 8 * 12, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    ctx->stats = dmann_stats{};
+    ctx->stats.n_in = n;
+    ctx->disc_timed = true;
+    ctx->stats_pending = true;
+    // observer: u = pos - opos gives -sum_i dL/du_i; the rotation adds
+    // sum_e dL/drot[e] * drot[e]/dopos when the frame came from
+    // dmann_set_observer (with dmann_set_frame the rotation is held fixed)
+    double jac[27] = {0};
+    const bool rot_terms =
+        ctx->have_geom && observer_rotation_jacobian(ctx->opos, ctx->cpos, ctx->align, jac);
+    for (int k = 0; k < 3; k++) {
+        double v = -ctx->h_oacc[k];
+        if (rot_terms)
+            for (int e = 0; e < 9; e++) v += ctx->h_oacc[3 + e] * jac[3 * e + k];
+        grad_opos[k] = v;
+    }
+    return collect_stats(ctx);
+}
+
 dmann_status dmann_observer_rotation(const double opos[3], const double cpos[3],
                                      const double align[3], double rot[9], double angles[2]) {
     if (!opos || !cpos || !align || !rot) return DMANN_ERR_INVALID;
@@ -678,6 +808,12 @@ dmann_status dmann_observer_rotation(const double opos[3], const double cpos[3],
         angles[1] = ph;
     }
     return DMANN_OK;
+}
+
+dmann_status dmann_observer_rotation_jacobian(const double opos[3], const double cpos[3],
+                                              const double align[3], double jac[27]) {
+    if (!opos || !cpos || !align || !jac) return DMANN_ERR_INVALID;
+    return observer_rotation_jacobian(opos, cpos, align, jac) ? DMANN_OK : DMANN_ERR_INVALID;
 }
 
 dmann_status dmann_code_units(double h100, double Lbox_in_Mpc, double mass_to_Msun, double out[9]) {

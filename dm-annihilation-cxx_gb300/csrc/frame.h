@@ -12,6 +12,13 @@ namespace dmann {
 bool observer_rotation(const double opos[3], const double cpos[3], const double align[3],
                        double rot[9], double *otheta, double *ophi);
 
+// d rot[e] / d opos[k] of observer_rotation, jac[3 e + k] (e the row-major
+// element index), by forward-mode differentiation of the same operations.
+// The roll angle's |.| and the degenerate-axis branch are differentiated
+// piecewise.  Returns false when opos == cpos.
+bool observer_rotation_jacobian(const double opos[3], const double cpos[3], const double align[3],
+                                double jac[27]);
+
 // Unit factor of the default flux law (src/flux/flux_ann_nosom.cpp:13-16)
 // from the code units of Parameters::setupUnits (src/parameters.cpp:42-82).
 struct CodeUnits {

@@ -36,7 +36,11 @@ struct PrepOut {
     double *theta, *phi, *ar, *flux;
     int *cpix;
     int *key;     // sort key, -1 for skipped / single-pixel particles
+    signed char *cls;  // optional (may be null): a PClass per particle
 };
+
+// Particle classes written to PrepOut::cls.
+enum PClass : signed char { PC_SKIPPED = 0, PC_INVALID = 1, PC_SINGLE = 2, PC_DISC = 3 };
 
 struct Accum {
     double *acc64;      // DMANN_PLAIN_F64
@@ -54,6 +58,7 @@ struct PrepArgs {
     Accum acc;
     int precision;
     int block_bucket_min;       // discs whose size bucket >= this go block-per-particle
+    int deposit_singles;        // 0: classify only (the adjoint), no map deposits
 };
 
 struct DiscArgs {
@@ -80,5 +85,12 @@ cudaError_t launch_disc_plain(const DiscArgs &a, int num_sms, int blocks_per_sm,
                               cudaEvent_t mid);
 cudaError_t launch_disc_comp(const DiscArgs &a, int num_sms, int blocks_per_sm, cudaStream_t s,
                              cudaEvent_t mid);
+// adjoint.cu: gradients of the plain-form map for dL/dmap = gmap; grad is
+// [6][n] (x, y, z, m, rho, h); oacc[12] (zeroed by the caller) receives
+// sum_i dL/du_i and dL/drot (row-major).  Needs the prep outputs (with cls)
+// and the disc queue of the same particles and frame.
+cudaError_t launch_adjoint(const DiscArgs &d, const Particles &p, const signed char *cls,
+                           const double *gmap, double *grad, double *oacc, int num_sms,
+                           cudaStream_t s);
 
 }  // namespace dmann

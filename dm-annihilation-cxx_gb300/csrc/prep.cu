@@ -114,6 +114,8 @@ __global__ void __launch_bounds__(256) k_prep(PrepArgs a) {
         } else {
             a.out.key[i] = -1;
         }
+        if (a.out.cls)
+            a.out.cls[i] = disc ? PC_DISC : single ? PC_SINGLE : invalid ? PC_INVALID : PC_SKIPPED;
     }
     count_warp(a.ctr + C_KEPT, kept);
     count_warp(a.ctr + C_SINGLE, single);
@@ -123,7 +125,9 @@ __global__ void __launch_bounds__(256) k_prep(PrepArgs a) {
     double fs = warp_sum(kept ? flux : 0.0);
     if ((threadIdx.x & 31) == 0 && fs != 0.0) atomicAdd(a.flux_sum, fs);
     // single-pixel particles: all their flux into the centre pixel
-    if (a.precision == 0) {
+    if (!a.deposit_singles) {
+        // classification only
+    } else if (a.precision == 0) {
         double *acc = a.acc.acc64;
         aggregated_add(single, cpix, flux, [acc](int p, double v) { red_add_f64(acc + p, v); });
     } else {

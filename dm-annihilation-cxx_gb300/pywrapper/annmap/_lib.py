@@ -66,7 +66,9 @@ SIGNATURES = {
     "dmann_get_stats": (C.c_int, [_P, C.POINTER(Stats)]),
     "dmann_render_batch": (C.c_int, [_P, _P, _P, _P, _P, _P, _P, C.c_int64, C.c_int, _D3, _D3,
                                      C.POINTER(C.c_int), C.c_int, C.POINTER(C.c_void_p)]),
+    "dmann_adjoint": (C.c_int, [_P, _P, _P, _P, _P, _P, _P, C.c_int64, C.c_int, _P, _P, _D3]),
     "dmann_observer_rotation": (C.c_int, [_D3, _D3, _D3, _D3, _D3]),
+    "dmann_observer_rotation_jacobian": (C.c_int, [_D3, _D3, _D3, _D3]),
     "dmann_code_units": (C.c_int, [C.c_double, C.c_double, C.c_double, _D3]),
     "dmann_hires_threshold": (C.c_double, [_D3, C.c_int]),
     "dmann_render_noalloc": (C.c_int, [_P, _P, _P, _P, _P, _P, C.c_int64, C.c_int, _D3, _D3,

@@ -178,6 +178,36 @@ class Renderer:
         self._keep = []
         return outs
 
+    def adjoint(self, parts: dict, nside: int, grad_map, out=None):
+        """Gradient of L = sum_p grad_map[p] * map[p] (the plain-form map of
+        ``render`` for this frame and these units) with respect to the particle
+        inputs and the observer position.  Returns (grad, grad_opos): grad is
+        [6, n] float64 (rows x, y, z, m, rho, h; a CUDA tensor when the inputs
+        are CUDA tensors, else numpy), grad_opos a length-3 numpy array."""
+        arrays = [parts[f] for f in FIELDS]
+        n = len(arrays[0])
+        if any(len(a) != n for a in arrays):
+            raise ValueError("particle arrays differ in length")
+        npix = 12 * int(nside) * int(nside)
+        if len(grad_map) != npix:
+            raise ValueError("grad_map has the wrong length")
+        self._keep = []
+        on_gpu = any(_is_torch(a) and a.is_cuda for a in arrays)
+        if out is None:
+            if on_gpu:
+                import torch
+                out = torch.empty((6, n), dtype=torch.float64, device=arrays[0].device)
+            else:
+                out = np.zeros((6, n), dtype=np.float64)
+        self._use_torch_stream(arrays + [grad_map, out])
+        ptrs = [self._ptr(a, np.float32) for a in arrays]
+        gm = self._ptr(grad_map, np.float64)
+        optr = C.c_void_p(out.data_ptr() if _is_torch(out) else out.ctypes.data)
+        go = (C.c_double * 3)()
+        self._check(self.L.dmann_adjoint(self.ctx, *ptrs, int(n), int(nside), gm, optr, go))
+        self._keep = []
+        return out, np.array(go[:])
+
     def synchronize(self):
         self._check(self.L.dmann_synchronize(self.ctx))
         self._keep = []

@@ -32,6 +32,8 @@
  *                                     src/genmap.cpp:67-169.
  *   dmann_render_batch                no reference counterpart (many
  *                                     observers / Nside values in one call)
+ *   dmann_adjoint                     no reference counterpart (gradients of
+ *                                     a pixelwise loss of the map)
  */
 #ifndef DMANN_H
 #define DMANN_H
@@ -170,6 +172,29 @@ dmann_status dmann_render_batch(dmann_ctx *ctx, const float *x, const float *y,
                                 const int *nside, int precision,
                                 double *const *maps);
 
+/* ---- differentiation ---- */
+/* Adjoint of dmann_render's plain FP64 form (no reference counterpart).
+ * grad_map[p] = dL/dmap[p] for a scalar loss L of the map dmann_render
+ * returns for these particles, this nside and the context's frame and units
+ * (12*nside^2 doubles, host or device).  Writes dL/d(particle inputs) into
+ * grad (6*n doubles, host or device, planes x, y, z, m, rho, h of n each)
+ * and dL/d(observer position) into grad_opos (host, 3 doubles).
+ *
+ * The derivative is that of the map with every particle's disc pixel set
+ * and single-pixel decision held fixed (the map is piecewise smooth: it
+ * jumps where a pixel centre crosses a disc edge).  Skipped particles (hires
+ * mass, rho < 0, invalid geometry) get zero gradient.  The kernel weights are
+ * recomputed in FP64, not stored.  The observer gradient includes the
+ * rotation's dependence on the observer when the frame was set by
+ * dmann_set_observer; after dmann_set_frame the rotation is held fixed.
+ * Blocks until the gradients are written; dmann_get_stats then reports the
+ * adjoint's counters and device time. */
+dmann_status dmann_adjoint(dmann_ctx *ctx, const float *x, const float *y,
+                           const float *z, const float *m, const float *rho,
+                           const float *h, int64_t n, int nside,
+                           const double *grad_map, double *grad,
+                           double grad_opos[3]);
+
 /* Statistics of the last completed map (synchronises the stream). */
 dmann_status dmann_get_stats(const dmann_ctx *ctx, dmann_stats *out);
 
@@ -210,6 +235,14 @@ dmann_status dmann_render_noalloc(const float *x, const float *y, const float *z
 dmann_status dmann_observer_rotation(const double opos[3], const double cpos[3],
                                      const double align[3], double rot[9],
                                      double angles[2]);
+/* d rot[e] / d opos[k] of dmann_observer_rotation as jac[3*e + k] (e the
+ * row-major element of rot), by forward-mode differentiation of the same
+ * operations (cpos and align held fixed).  DMANN_ERR_INVALID when
+ * opos == cpos. */
+dmann_status dmann_observer_rotation_jacobian(const double opos[3],
+                                              const double cpos[3],
+                                              const double align[3],
+                                              double jac[27]);
 /* Parameters::setupUnits (src/parameters.cpp:42-82) and the default flux
  * law's unit factor (src/flux/flux_ann_nosom.cpp:13-16).  out = {rho_crit,
  * length_to_cgs, time_to_cgs, density_to_cgs, mass_to_cgs, mass_to_Msun,

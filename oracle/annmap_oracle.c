@@ -150,26 +150,33 @@ typedef struct {
     int kept;
 } geom_t;
 
-/* genmap.cpp:82-106 for one particle */
-static void particle_geom(const orc_params *p, const orc_hpx *hb, float mass,
-                          float dens, float hsmooth, float px, float py,
-                          float pz, geom_t *g) {
+/* genmap.cpp:82-106 for one particle.  The inputs are the float values
+ * promoted to double (the finite-difference checks pass unrounded doubles). */
+static void particle_geom_d(const orc_params *p, const orc_hpx *hb, double mass,
+                            double dens, double hsmooth, double px, double py,
+                            double pz, geom_t *g) {
     g->kept = 0;
-    if ((double)mass >= p->hires_threshold || dens < 0) return;
+    if (mass >= p->hires_threshold || dens < 0) return;
     g->kept = 1;
     double ox = p->obs_pos[0], oy = p->obs_pos[1], oz = p->obs_pos[2];
-    double dx = (double)px - ox, dy = (double)py - oy, dz = (double)pz - oz;
+    double dx = px - ox, dy = py - oy, dz = pz - oz;
     g->d = sqrt(dx * dx + dy * dy + dz * dz);
     /* flux_ann_nosom.cpp:18: unit_factor * dens * mass / (4 PI d d) */
-    g->flux = p->unit_factor * (double)dens * (double)mass /
-              (4.0 * PI * g->d * g->d);
+    g->flux = p->unit_factor * dens * mass / (4.0 * PI * g->d * g->d);
     calc_angles(dx, dy, dz, g->d, p, &g->costheta, &g->phi);
     double ct = g->costheta;
     if (ct > 1.0) ct = 1.0; /* acos argument guard */
     if (ct < -1.0) ct = -1.0;
     g->theta = acos(ct);
-    g->ar = (double)hsmooth / g->d;
+    g->ar = hsmooth / g->d;
     g->pix = orc_hpx_ang2pix(hb, g->theta, g->phi);
+}
+
+static void particle_geom(const orc_params *p, const orc_hpx *hb, float mass,
+                          float dens, float hsmooth, float px, float py,
+                          float pz, geom_t *g) {
+    particle_geom_d(p, hb, (double)mass, (double)dens, (double)hsmooth,
+                    (double)px, (double)py, (double)pz, g);
 }
 
 void orc_particle_geom(const orc_params *p, float mass, float dens,
@@ -333,4 +340,163 @@ double orc_finalize(const orc_params *p, double *map) {
         map[i] /= p->dOmega;
     }
     return totalC;
+}
+
+/* ------------------------------------------------------------------ adjoint
+ * The derivative of L = sum_p G[p] map[p] (map after the dOmega division)
+ * with the disc pixel sets held fixed; see oracle.h for the formulas. */
+
+/* Disc pixels and weights of one kept particle; returns the pixel count, or
+ * -1 for a single-pixel deposit (genmap.cpp:107-128). */
+static int64_t disc_pixels(const orc_params *p, const orc_hpx *hb, const geom_t *g,
+                           int32_t *list) {
+    if (2.0 * g->ar < p->theta0) return -1;
+    int64_t npd = orc_hpx_query_disc_list(hb, g->theta, g->phi, 2.0 * g->ar, list);
+    return npd < 2 ? -1 : npd;
+}
+
+static void ang2vec(const geom_t *g, double v[3]) {
+    double sz = sin(g->theta);
+    v[0] = sz * cos(g->phi);
+    v[1] = sz * sin(g->phi);
+    v[2] = cos(g->theta);
+}
+
+/* w of one disc pixel exactly as genmap.cpp:133-143 computes it; also
+ * returns the pixel vector and the angle. */
+static double pixel_weight(const orc_hpx *hb, int32_t pix, const double v[3], double ar,
+                           double pv[3], double *alpha, double *dotc) {
+    orc_hpx_pix2vec(hb, pix, pv);
+    double dot = pv[0] * v[0] + pv[1] * v[1] + pv[2] * v[2];
+    if (dot > 1.0) dot = 1.0;
+    if (dot < -1.0) dot = -1.0;
+    double a = acos(dot);
+    double d2 = a / ar;
+    d2 = d2 * d2;
+    *alpha = a;
+    *dotc = dot;
+    return exp(-0.5 * d2 / 0.333);
+}
+
+double orc_particle_loss(const orc_params *p, double mass, double dens, double hsmooth,
+                         double x, double y, double z, const double *G, uint64_t *sig) {
+    orc_hpx hb;
+    orc_hpx_init(&hb, p->nside);
+    geom_t g;
+    memset(&g, 0, sizeof g);
+    particle_geom_d(p, &hb, mass, dens, hsmooth, x, y, z, &g);
+    uint64_t hsig = 1469598103934665603ull; /* FNV-1a over the branch and pixels */
+#define SIG(v) do { hsig ^= (uint64_t)(v); hsig *= 1099511628211ull; } while (0)
+    double L = 0.0;
+    if (!g.kept || !(g.d > 0.0)) {
+        SIG(0);
+    } else {
+        int32_t *list = (int32_t *)malloc(sizeof(int32_t) * (size_t)p->npix);
+        int64_t npd = list ? disc_pixels(p, &hb, &g, list) : -1;
+        if (npd < 0) {
+            SIG(1);
+            SIG(g.pix);
+            L = G[g.pix] * g.flux / p->dOmega;
+        } else {
+            double v[3];
+            ang2vec(&g, v);
+            SIG(2);
+            double S = 0.0;
+            for (int64_t j = 0; j < npd; j++) {
+                double pv[3], a, dc;
+                S += pixel_weight(&hb, list[j], v, g.ar, pv, &a, &dc);
+                SIG(list[j]);
+            }
+            for (int64_t j = 0; j < npd; j++) {
+                double pv[3], a, dc;
+                double w = pixel_weight(&hb, list[j], v, g.ar, pv, &a, &dc);
+                L += G[list[j]] * ((w / S) * g.flux) / p->dOmega;
+            }
+        }
+        free(list);
+    }
+#undef SIG
+    if (sig) *sig = hsig;
+    return L;
+}
+
+void orc_particle_losses(const orc_params *p, const double *mass, const double *dens,
+                         const double *hsmooth, const double *x, const double *y,
+                         const double *z, int64_t n, const double *G, double *L,
+                         uint64_t *sig) {
+    for (int64_t i = 0; i < n; i++)
+        L[i] = orc_particle_loss(p, mass[i], dens[i], hsmooth[i], x[i], y[i], z[i], G,
+                                 sig ? sig + i : NULL);
+}
+
+int orc_adjoint(const orc_params *p, const float *mass, const float *dens,
+                const float *hsmooth, const float *x, const float *y, const float *z,
+                int64_t n, const double *G, double *grad, double oacc[12]) {
+    orc_hpx hb;
+    orc_hpx_init(&hb, p->nside);
+    int32_t *list = (int32_t *)malloc(sizeof(int32_t) * (size_t)p->npix);
+    if (!list) return -1;
+    const double inv_dO = 1.0 / p->dOmega;
+    for (int k = 0; k < 12; k++) oacc[k] = 0.0;
+    for (int64_t i = 0; i < n; i++) {
+        for (int k = 0; k < 6; k++) grad[k * n + i] = 0.0;
+        geom_t g;
+        particle_geom(p, &hb, mass[i], dens[i], hsmooth[i], x[i], y[i], z[i], &g);
+        if (!g.kept || !(g.d > 0.0) || !isfinite(g.flux) || !isfinite(g.ar)) continue;
+        double Gb, KT = 0.0, KV[3] = {0.0, 0.0, 0.0};
+        int64_t npd = disc_pixels(p, &hb, &g, list);
+        if (npd < 0) {
+            Gb = G[g.pix] * inv_dO;
+        } else {
+            double v[3];
+            ang2vec(&g, v);
+            double S = 0.0, A = 0.0;
+            for (int64_t j = 0; j < npd; j++) {
+                double pv[3], a, dc;
+                double w = pixel_weight(&hb, list[j], v, g.ar, pv, &a, &dc);
+                S += w;
+                A += G[list[j]] * w;
+            }
+            double Gm = A / S;
+            double V[3] = {0.0, 0.0, 0.0}, T = 0.0;
+            for (int64_t j = 0; j < npd; j++) {
+                double pv[3], a, dc;
+                double w = pixel_weight(&hb, list[j], v, g.ar, pv, &a, &dc);
+                double q = (G[list[j]] - Gm) * w;
+                double e[3] = {pv[0] - dc * v[0], pv[1] - dc * v[1], pv[2] - dc * v[2]};
+                double sa = sqrt(e[0] * e[0] + e[1] * e[1] + e[2] * e[2]);
+                double f = sa > 0.0 ? q * a / sa : 0.0;
+                for (int k = 0; k < 3; k++) V[k] += f * e[k];
+                T += q * a * a;
+            }
+            double K = (1.0 / 0.333) * g.flux / (S * g.ar * g.ar) * inv_dO;
+            Gb = Gm * inv_dO;
+            KT = K * T;
+            for (int k = 0; k < 3; k++) KV[k] = K * V[k];
+        }
+        double u[3] = {(double)x[i] - p->obs_pos[0], (double)y[i] - p->obs_pos[1],
+                       (double)z[i] - p->obs_pos[2]};
+        double d = g.d;
+        double uh[3] = {u[0] / d, u[1] / d, u[2] / d};
+        double fd = p->unit_factor / (4.0 * PI * d * d);
+        double F = fd * (double)dens[i] * (double)mass[i];
+        double w[3] = {-KV[0], -KV[1], KV[2]}; /* D K V, D = diag(-1,-1,1) */
+        double cr = -(2.0 * Gb * F + KT) / d;
+        for (int j = 0; j < 3; j++) {
+            double rw = p->rotmatrix[j][0] * w[0] + p->rotmatrix[j][1] * w[1] +
+                        p->rotmatrix[j][2] * w[2];
+            double gj = cr * uh[j] + rw / d;
+            grad[j * n + i] = gj;
+            oacc[j] += gj;
+        }
+        grad[3 * n + i] = Gb * fd * (double)dens[i];
+        grad[4 * n + i] = Gb * fd * (double)mass[i];
+        if (npd >= 0) {
+            grad[5 * n + i] = KT / (double)hsmooth[i];
+            for (int j = 0; j < 3; j++)
+                for (int k = 0; k < 3; k++) oacc[3 + 3 * j + k] += uh[j] * w[k];
+        }
+    }
+    free(list);
+    return 0;
 }

@@ -109,6 +109,40 @@ double orc_finalize(const orc_params *p, double *map);
 void orc_particle_geom(const orc_params *p, float mass, float dens,
                        float hsmooth, float x, float y, float z, double out[8]);
 
+/* ---------------- the adjoint (FP64 CPU reference) ----------------
+ * Loss L = sum_p G[p] map[p], map as orc_finalize leaves it (divided by
+ * dOmega).  For one kept particle with u = pos - opos, d = |u|,
+ * F = unit_factor rho m / (4 pi d^2), ar = h/d, direction n (ang2vec of the
+ * particle's theta, phi: n = D R^T u / d with D = diag(-1, -1, 1), the pi
+ * shift of phi) and disc weights w_p = exp(-c alpha_p^2 / ar^2), c = 0.5/0.333,
+ * alpha_p = acos(v_p . n), S = sum w_p, the map gets F w_p / S / dOmega.
+ * With g = G / dOmega, Gb = sum g_p w_p / S, q_p = (g_p - Gb) w_p,
+ * V = sum q_p alpha_p / sin(alpha_p) (v_p - cos(alpha_p) n), T = sum q_p alpha_p^2
+ * and K = 2 c F / (S ar^2):
+ *   dL/dm = Gb F/m,  dL/drho = Gb F/rho,  dL/dh = K T / h,
+ *   dL/dpos = -(2 Gb F + K T)/d u/d + (K/d) R D V,
+ *   dL/drot[j][a] = K (D V)_a u_j / d.
+ * A single-pixel deposit has Gb = g[cpix] and V = T = 0.  The pixel sets are
+ * held fixed. */
+
+/* L_i of one particle from double inputs (no float rounding), and in *sig
+ * (may be NULL) a hash of its branch and pixel set: the finite-difference
+ * checks use it to confirm the set did not change between the two sides. */
+double orc_particle_loss(const orc_params *p, double mass, double dens, double hsmooth,
+                         double x, double y, double z, const double *G, uint64_t *sig);
+
+/* orc_particle_loss over n particles (double SoA inputs). */
+void orc_particle_losses(const orc_params *p, const double *mass, const double *dens,
+                         const double *hsmooth, const double *x, const double *y,
+                         const double *z, int64_t n, const double *G, double *L,
+                         uint64_t *sig);
+
+/* grad = [6][n] (x, y, z, m, rho, h); oacc[0..2] = sum_i dL/du_i,
+ * oacc[3..11] = dL/drot (row-major).  Returns 0 on success. */
+int orc_adjoint(const orc_params *p, const float *mass, const float *dens,
+                const float *hsmooth, const float *x, const float *y, const float *z,
+                int64_t n, const double *G, double *grad, double oacc[12]);
+
 #ifdef __cplusplus
 }
 #endif

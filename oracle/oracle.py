@@ -91,6 +91,15 @@ def lib():
             L.orc_finalize.restype = C.c_double
             L.orc_particle_geom.argtypes = [P(OrcParams), C.c_float, C.c_float, C.c_float,
                                             C.c_float, C.c_float, C.c_float, P(C.c_double)]
+            L.orc_particle_loss.argtypes = [P(OrcParams)] + [C.c_double] * 6 + [
+                P(C.c_double), P(C.c_uint64)]
+            L.orc_particle_loss.restype = C.c_double
+            d64 = P(C.c_double)
+            L.orc_particle_losses.argtypes = [P(OrcParams), d64, d64, d64, d64, d64, d64,
+                                              C.c_int64, d64, d64, P(C.c_uint64)]
+            L.orc_adjoint.argtypes = [P(OrcParams), f32, f32, f32, f32, f32, f32, C.c_int64,
+                                      P(C.c_double), P(C.c_double), P(C.c_double)]
+            L.orc_adjoint.restype = C.c_int
             _LIB = L
     return _LIB
 
@@ -192,3 +201,83 @@ def particle_geom(p: OrcParams, m, rho, h, x, y, z) -> dict:
     lib().orc_particle_geom(C.byref(p), m, rho, h, x, y, z, out)
     keys = ("d", "flux", "costheta", "phi", "theta", "ar", "pix", "kept")
     return dict(zip(keys, out[:]))
+
+
+# ---------------------------------------------------------------- adjoint
+def _dptr(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def adjoint(p: OrcParams, parts: dict, G) -> tuple:
+    """FP64 CPU reference adjoint of L = sum_p G[p] map[p] (map after the
+    dOmega division).  Returns (grad [6, n] for x, y, z, m, rho, h,
+    oacc[12] = (sum_i dL/du_i, dL/drot row-major))."""
+    keep, ptrs = [], []
+    for k in ("m", "rho", "h", "x", "y", "z"):
+        a, ptr = _f32(parts[k])
+        keep.append(a)
+        ptrs.append(ptr)
+    n = len(keep[0])
+    G = np.ascontiguousarray(G, dtype=np.float64)
+    grad = np.zeros((6, n), dtype=np.float64)
+    oacc = np.zeros(12, dtype=np.float64)
+    rc = lib().orc_adjoint(C.byref(p), *ptrs, n, _dptr(G), _dptr(grad), _dptr(oacc))
+    if rc != 0:
+        raise RuntimeError("oracle adjoint failed")
+    return grad, oacc
+
+
+def particle_loss(p: OrcParams, m, rho, h, x, y, z, G) -> tuple:
+    """(L_i, pixel-set signature) of one particle from double inputs."""
+    sig = C.c_uint64()
+    L = lib().orc_particle_loss(C.byref(p), float(m), float(rho), float(h), float(x), float(y),
+                                float(z), _dptr(G), C.byref(sig))
+    return L, sig.value
+
+
+def particle_losses(p: OrcParams, parts: dict, G) -> tuple:
+    """(L_i, signature_i) of every particle; ``parts`` may hold float64
+    arrays (unrounded inputs for finite differences)."""
+    arrs = [np.ascontiguousarray(parts[k], dtype=np.float64) for k in ("m", "rho", "h", "x", "y", "z")]
+    n = len(arrs[0])
+    G = np.ascontiguousarray(G, dtype=np.float64)
+    L = np.zeros(n)
+    sig = np.zeros(n, dtype=np.uint64)
+    lib().orc_particle_losses(C.byref(p), *[_dptr(a) for a in arrs], n, _dptr(G), _dptr(L),
+                              sig.ctypes.data_as(C.POINTER(C.c_uint64)))
+    return L, sig
+
+
+def with_observer(p: OrcParams, obs_pos) -> OrcParams:
+    """A copy of p with another observer position (all derived fields redone)."""
+    q = OrcParams()
+    C.memmove(C.byref(q), C.byref(p), C.sizeof(OrcParams))
+    for i in range(3):
+        q.obs_pos[i] = float(obs_pos[i])
+    lib().orc_params_setup(C.byref(q))
+    return q
+
+
+def rotation_jacobian_fd(p: OrcParams, rel_step: float = 1e-4) -> np.ndarray:
+    """d rotmatrix / d obs_pos by central differences of the parameter set-up
+    with one Richardson step: jac[e, k] for the row-major element e."""
+    o = np.array(p.obs_pos[:], dtype=np.float64)
+    radius = np.linalg.norm(o - np.array(p.centerpos[:]))
+    jac = np.zeros((9, 3))
+    for k in range(3):
+        def D(step):
+            op, om = o.copy(), o.copy()
+            op[k] += step
+            om[k] -= step
+            return (rotmatrix(with_observer(p, op)) - rotmatrix(with_observer(p, om))).reshape(9) / (2 * step)
+        hstep = rel_step * radius
+        jac[:, k] = (4.0 * D(hstep / 2) - D(hstep)) / 3.0
+    return jac
+
+
+def observer_grad(p: OrcParams, oacc, jac=None) -> np.ndarray:
+    """dL/d(observer position) from the adjoint's sums: -sum_i dL/du_i plus
+    the rotation's dependence on the observer."""
+    if jac is None:
+        jac = rotation_jacobian_fd(p)
+    return -np.asarray(oacc[:3]) + np.asarray(oacc[3:]) @ jac

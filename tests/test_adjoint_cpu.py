@@ -1,0 +1,95 @@
+"""CPU checks of the adjoint's references: the oracle's FP64 adjoint against
+central finite differences of its own forward map (per particle and for the
+observer position), and the library's forward-mode rotation Jacobian against
+finite differences of the oracle's parameter set-up."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+import oracle as O
+from adjoint_cases import FIELDS, fd_check, loss_grad, make_case, observer_fd
+
+
+@pytest.fixture(scope="module")
+def case():
+    P, parts, p = make_case(3000, 128, single_frac=0.2, skipped=40)
+    mp, st, _ = O.render(p, parts)
+    assert st["single_small"] > 300 and st["disc"] > 1000 and st["skipped"] == 40
+    target, _, _ = O.render(p, __import__("adjoint_cases").jittered(P))
+    _, G = loss_grad(mp, target)
+    grad, oacc = O.adjoint(p, parts, G)
+    return P, parts, p, G, grad, oacc
+
+
+def test_oracle_adjoint_matches_central_differences(case):
+    P, parts, p, G, grad, oacc = case
+    res = fd_check(p, parts, G, grad)
+    for k in FIELDS:
+        err, n_ok = res[k]
+        assert n_ok > 2500, (k, n_ok)
+        assert err < 1e-6, (k, err)
+
+
+def test_oracle_adjoint_zero_for_skipped_particles(case):
+    P, parts, p, G, grad, oacc = case
+    skipped = (parts["rho"] < 0) | (parts["m"].astype(np.float64) >= p.hires_threshold)
+    assert skipped.sum() == 40
+    assert np.all(grad[:, skipped] == 0.0)
+    assert np.all(np.isfinite(grad))
+
+
+def test_oracle_observer_gradient_matches_central_differences(case):
+    P, parts, p, G, grad, oacc = case
+    fd, keep = observer_fd(p, parts, G)
+    assert keep.sum() > 0.95 * len(keep)
+    sub = {k: np.asarray(parts[k])[keep] for k in FIELDS}
+    _, oa = O.adjoint(p, sub, G)
+    go = O.observer_grad(p, oa)
+    assert np.linalg.norm(go - fd) < 1e-6 * np.linalg.norm(fd)
+
+
+def test_euler_identities_of_the_oracle_adjoint(case):
+    """The map is linear in m and in rho, and scaling every offset from the
+    observer and every h by s scales it by s^-2, so with L = sum G map:
+    sum m dL/dm = sum rho dL/drho = L and sum (u . dL/du + h dL/dh) = -2 L."""
+    P, parts, p, G, grad, oacc = case
+    mp, _, _ = O.render(p, parts)
+    L = float(np.dot(G, mp))
+    o = np.array(p.obs_pos[:])
+    u = np.stack([parts[k].astype(np.float64) - o[i] for i, k in enumerate(("x", "y", "z"))])
+    m, rho, h = (parts[k].astype(np.float64) for k in ("m", "rho", "h"))
+    assert np.sum(m * grad[3]) == pytest.approx(L, rel=1e-10)
+    assert np.sum(rho * grad[4]) == pytest.approx(L, rel=1e-10)
+    assert np.sum(u * grad[:3]) + np.sum(h * grad[5]) == pytest.approx(-2 * L, rel=1e-9)
+
+
+def test_rotation_jacobian_matches_central_differences():
+    from annmap import _lib
+    L = _lib.load()
+    # (points off the kinks of the roll angle |atan2(.)|, where only one-sided
+    # derivatives exist)
+    for opos, cpos, align in [((4.6, 4.6, 4.6), (0, 0, 0), (0, 0, 1)),
+                              ((-3.0, 7.0, 1.5), (0.5, -0.2, 0.1), (0.3, 0.4, 0.866)),
+                              ((8.0, 0.7, 0.1), (0, 0, 0), (0, 1, 0))]:
+        p = O.make_params(nside=8, obs_pos=opos, centerpos=cpos, align_vec=align)
+        jac = (C.c_double * 27)()
+        d3 = lambda v: (C.c_double * 3)(*[float(a) for a in v])
+        assert L.dmann_observer_rotation_jacobian(d3(opos), d3(cpos), d3(align), jac) == 0
+        J = np.array(jac[:]).reshape(9, 3)
+        Jfd = O.rotation_jacobian_fd(p)
+        assert np.max(np.abs(J - Jfd)) < 1e-8 * max(1.0, np.max(np.abs(Jfd)))
+        rot = (C.c_double * 9)()
+        assert L.dmann_observer_rotation(d3(opos), d3(cpos), d3(align), rot, None) == 0
+        assert np.array_equal(np.array(rot[:]).reshape(3, 3), O.rotmatrix(p))  # bit for bit
+    jac = (C.c_double * 27)()
+    z = (C.c_double * 3)(0, 0, 0)
+    assert L.dmann_observer_rotation_jacobian(z, z, (C.c_double * 3)(0, 0, 1), jac) == 1
+
+
+def test_sky_map_rejects_cpu_tensors():
+    torch = pytest.importorskip("torch")
+    from annmap.autograd import sky_map
+    t = torch.zeros(4)
+    with pytest.raises(ValueError):
+        sky_map(t, t, t, t, t, t, torch.zeros(3, dtype=torch.float64), nside=4)

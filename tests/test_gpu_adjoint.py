@@ -1,0 +1,172 @@
+"""GPU adjoint (dmann_adjoint through the C ABI, and the torch.autograd
+Function over it) against its references.
+
+  * the oracle's FP64 CPU adjoint on the same float inputs: the same
+    formulas, different summation order -- norm-wise relative error per
+    input field <= 1e-9;
+  * FP64 central differences of the oracle's forward loss, per particle,
+    with particles whose pixel set changes between the two sides left out:
+    norm-wise relative error per field <= 1e-6 (the adjoint's target);
+  * the observer gradient (forward-mode rotation Jacobian on the GPU side,
+    finite-difference Jacobian on the oracle side) <= 1e-8 of the oracle's,
+    and <= 1e-6 of central differences of the summed loss;
+  * at the full adjoint workload (4,194,304 particles, Nside 512) the
+    size-independent Euler identities of the map: it is linear in m and in
+    rho, and homogeneous of degree -2 in (pos - opos, h), so
+    sum m dL/dm = sum rho dL/drho = L and sum (u . dL/du + h dL/dh) = -2 L.
+"""
+import numpy as np
+import pytest
+
+import annmap
+import oracle as O
+from adjoint_cases import FIELDS, N_FULL, fd_check, jittered, loss_grad, make_case, observer_fd
+from annmap import synth
+
+pytestmark = pytest.mark.gpu
+
+PLAIN = annmap.PLAIN_F64
+
+
+def _renderer_for(P, p):
+    r = annmap.Renderer(0)
+    r.set_observer(P.obs_pos, P.centerpos, P.align_vec)
+    r.set_units(p.unit_factor, p.hires_threshold)
+    return r
+
+
+def _normwise(a, b):
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+@pytest.fixture(scope="module")
+def case():
+    P, parts, p = make_case(20000, 128, single_frac=0.2, skipped=100)
+    r = _renderer_for(P, p)
+    mp = r.render(parts, 128, PLAIN)
+    target = r.render(jittered(P), 128, PLAIN)
+    _, G = loss_grad(mp, target)
+    grad, gopos = r.adjoint(parts, 128, G)
+    st = r.stats()
+    r.close()
+    return P, parts, p, G, grad, gopos, st
+
+
+def test_adjoint_counts(case):
+    P, parts, p, G, grad, gopos, st = case
+    assert st["n_in"] == 20000
+    assert st["n_kept"] == 20000 - 100
+    assert st["n_single"] > 3000 and st["n_disc"] > 10000
+    assert st["n_single"] + st["n_disc"] == st["n_kept"]
+
+
+def test_adjoint_matches_oracle_adjoint(case):
+    P, parts, p, G, grad, gopos, st = case
+    ref, oacc = O.adjoint(p, parts, G)
+    assert np.all(np.isfinite(grad))
+    skipped = (parts["rho"] < 0) | (parts["m"].astype(np.float64) >= p.hires_threshold)
+    assert np.all(grad[:, skipped] == 0.0)
+    for k, f in enumerate(FIELDS):
+        assert _normwise(grad[k], ref[k]) <= 1e-9, (f, _normwise(grad[k], ref[k]))
+    go_ref = O.observer_grad(p, oacc)
+    assert np.linalg.norm(gopos - go_ref) <= 1e-8 * np.linalg.norm(go_ref), (gopos, go_ref)
+
+
+def test_adjoint_matches_central_differences(case):
+    P, parts, p, G, grad, gopos, st = case
+    res = fd_check(p, parts, G, grad)
+    for f in FIELDS:
+        err, n_ok = res[f]
+        assert n_ok > 0.95 * len(P), (f, n_ok)
+        assert err <= 1e-6, (f, err)
+
+
+def test_observer_gradient_matches_central_differences(case):
+    P, parts, p, G, grad, gopos, st = case
+    fd, keep = observer_fd(p, parts, G)
+    assert keep.sum() > 0.95 * len(keep)
+    sub = {k: np.asarray(parts[k])[keep] for k in FIELDS}
+    r = _renderer_for(P, p)
+    _, go = r.adjoint(sub, 128, G)
+    r.close()
+    assert np.linalg.norm(go - fd) <= 1e-6 * np.linalg.norm(fd), (go, fd)
+
+
+def test_adjoint_host_and_device_buffers_agree(case):
+    torch = pytest.importorskip("torch")
+    P, parts, p, G, grad, gopos, st = case
+    r = _renderer_for(P, p)
+    tparts = {k: torch.from_numpy(np.asarray(v)).cuda() for k, v in parts.items()}
+    g2, go2 = r.adjoint(tparts, 128, torch.from_numpy(G).cuda())
+    torch.cuda.synchronize()
+    r.close()
+    assert np.array_equal(g2.cpu().numpy(), grad)   # per-particle sums have a fixed order
+    assert np.allclose(go2, gopos, rtol=1e-12, atol=0)
+
+
+def test_adjoint_with_fixed_rotation_frame(case):
+    """After dmann_set_frame the rotation does not follow the observer: the
+    observer gradient is then minus the sum of the position gradients."""
+    P, parts, p, G, grad, gopos, st = case
+    r = annmap.Renderer(0)
+    r.set_frame(O.rotmatrix(p), P.obs_pos)
+    r.set_units(p.unit_factor, p.hires_threshold)
+    g2, go2 = r.adjoint(parts, 128, G)
+    r.close()
+    assert np.array_equal(g2, grad)
+    assert np.allclose(go2, -grad[:3].sum(axis=1), rtol=1e-10, atol=0)
+
+
+def test_adjoint_empty_and_invalid_arguments():
+    P, parts, p = make_case(100, 16)
+    r = _renderer_for(P, p)
+    empty = {k: np.zeros(0, dtype=np.float32) for k in FIELDS}
+    g, go = r.adjoint(empty, 16, np.ones(12 * 16 * 16))
+    assert g.shape == (6, 0) and np.all(go == 0.0)
+    with pytest.raises(ValueError):
+        r.adjoint(parts, 16, np.ones(10))
+    with pytest.raises(annmap.DmannError):
+        r.adjoint(parts, 0, np.ones(0))
+    r.close()
+
+
+def test_sky_map_autograd_function(case):
+    torch = pytest.importorskip("torch")
+    from annmap.autograd import sky_map
+    P, parts, p, G, grad, gopos, st = case
+    t = {k: torch.from_numpy(np.asarray(v)).cuda().requires_grad_(True) for k, v in parts.items()}
+    opos = torch.tensor(P.obs_pos, dtype=torch.float64, requires_grad=True)
+    mp = sky_map(t["x"], t["y"], t["z"], t["m"], t["rho"], t["h"], opos, nside=128,
+                 cpos=P.centerpos, align=P.align_vec, unit_factor=p.unit_factor,
+                 hires_threshold=p.hires_threshold)
+    loss = (torch.from_numpy(G).cuda() * mp).sum()
+    loss.backward()
+    for k, f in enumerate(FIELDS):
+        got = t[f].grad.cpu().numpy().astype(np.float64)
+        assert t[f].grad.dtype == torch.float32
+        assert _normwise(got, grad[k].astype(np.float32).astype(np.float64)) == 0.0, f
+    assert np.allclose(opos.grad.numpy(), gopos, rtol=1e-12, atol=0)
+
+
+def test_adjoint_full_workload_euler_identities():
+    P, nside = synth.workload("nfw4m_sub20_adjoint")
+    assert len(P) == N_FULL and nside == 512
+    p = O.make_params(nside=nside, obs_pos=P.obs_pos, centerpos=P.centerpos,
+                      align_vec=P.align_vec, particle_masses=(P.particle_mass,))
+    parts = P.as_dict()
+    r = _renderer_for(P, p)
+    mp = r.render(parts, nside, PLAIN)
+    target = r.render(jittered(P), nside, PLAIN)
+    _, G = loss_grad(mp, target)
+    grad, gopos = r.adjoint(parts, nside, G)
+    st = r.stats()
+    r.close()
+    assert st["n_kept"] == N_FULL and st["n_disc"] > 0
+    assert np.all(np.isfinite(grad)) and np.all(np.isfinite(gopos))
+    L = float(np.dot(G, mp))
+    o = np.array(P.obs_pos)
+    u = np.stack([parts[k].astype(np.float64) - o[i] for i, k in enumerate(("x", "y", "z"))])
+    m, rho, h = (parts[k].astype(np.float64) for k in ("m", "rho", "h"))
+    assert np.sum(m * grad[3]) == pytest.approx(L, rel=1e-9)
+    assert np.sum(rho * grad[4]) == pytest.approx(L, rel=1e-9)
+    assert np.sum(u * grad[:3]) + np.sum(h * grad[5]) == pytest.approx(-2 * L, rel=1e-8)
