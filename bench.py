@@ -347,8 +347,77 @@ def run_gb300(args, ws, rank, local):
             line["px_err_vs_oracle"] = {"particles": cpu["particles"], "median": med2, "max": mx2,
                                         "total_flux_rel": abs(g.sum() * dom - otot) / otot}
     r.close()
+    if not args.no_extras and rank == 0:
+        del dparts, dmap
+        torch.cuda.empty_cache()
+        line["batched"] = bench_batched(dev)
+        line["adjoint"] = bench_adjoint(dev)
     if rank == 0:
         print(json.dumps(line), flush=True)
+
+
+def bench_batched(dev):
+    """64 observers on the 8 kpc sphere, Nside cycling 256/512/1024, all maps
+    of the 8,388,608-particle set rendered by one dmann_render_batch call
+    (one CUDA graph; inputs and maps on the device)."""
+    import torch
+    import annmap
+    from annmap import synth
+    P, _ = synth.workload("nfw8m_sub50_batched")
+    obs = synth.batched_observers(64)
+    par = annmap.Parameters.for_synthetic(P, 1024)
+    dparts = {k: torch.from_numpy(v).to(dev) for k, v in P.as_dict().items()}
+    frames, nsides = [], []
+    for opos, ns in obs:
+        par.set_observer(opos)
+        frames.append((np.array(par.rot_flat()), opos))
+        nsides.append(ns)
+    outs = [torch.empty(12 * ns * ns, dtype=torch.float64, device=dev) for ns in nsides]
+    r = annmap.Renderer(dev.index or 0)
+    r.set_params(par)
+    r.render_batch(dparts, frames, nsides, annmap.COMP_F32, outs=outs)   # warm-up
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    r.render_batch(dparts, frames, nsides, annmap.COMP_F32, outs=outs)
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t0
+    r.close()
+    return {"workload": "nfw8m_sub50_batched", "particles": len(P), "observers": len(obs),
+            "nsides": sorted(set(nsides)), "form": "compensated FP32", "seconds": dt,
+            "maps_per_s": len(obs) / dt, "particle_maps_per_s": len(P) * len(obs) / dt,
+            "launch": "one CUDA graph (dmann_render_batch, device maps)"}
+
+
+def bench_adjoint(dev):
+    """dmann_adjoint on the 4,194,304-particle set at Nside 512 (device
+    inputs, device gradient), after one warm-up call."""
+    import torch
+    import annmap
+    from annmap import synth
+    P, nside = synth.workload("nfw4m_sub20_adjoint")
+    par = annmap.Parameters.for_synthetic(P, nside)
+    dparts = {k: torch.from_numpy(v).to(dev) for k, v in P.as_dict().items()}
+    G = torch.randn(12 * nside * nside, dtype=torch.float64, device=dev,
+                    generator=torch.Generator(device=dev).manual_seed(7))
+    out = torch.empty((6, len(P)), dtype=torch.float64, device=dev)
+    r = annmap.Renderer(dev.index or 0)
+    r.set_observer(P.obs_pos, P.centerpos, P.align_vec)
+    r.set_units(par.unit_factor, par.hires_threshold)
+    r.set_stream(torch.cuda.current_stream(dev))
+    r.adjoint(dparts, nside, G, out=out)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    r.adjoint(dparts, nside, G, out=out)
+    dt = time.perf_counter() - t0
+    st = r.stats()
+    fwd = torch.empty(12 * nside * nside, dtype=torch.float64, device=dev)
+    r.render(dparts, nside, annmap.PLAIN_F64, out=fwd)
+    fst = r.stats()
+    r.close()
+    return {"workload": "nfw4m_sub20_adjoint", "particles": len(P), "nside": nside,
+            "ms": dt * 1e3, "kernel_ms": st["kernel_ms"], "particles_per_s": len(P) / dt,
+            "deposits": st["deposits"], "plain_forward_kernel_ms": fst["kernel_ms"],
+            "form": "FP64 adjoint of the plain form (two passes per disc)"}
 
 
 def main():
