@@ -157,6 +157,20 @@ def profile_traffic():
     return None
 
 
+def measure_l2_red(device, nbytes=400_000_000):
+    """Live L2 reduction rates (operations/s) of the library's own sweep
+    microbenchmark over a 400 MB array: FP32 red and the compensated deposit."""
+    import ctypes as C
+    from annmap import _lib
+    L = _lib.load()
+    out = {}
+    for name, kind, reps in (("red_f32", 0, 20), ("comp_f32", 2, 10), ("red_f64", 1, 20)):
+        v = C.c_double()
+        st = L.dmann_measure_l2_red(int(device), kind, int(nbytes), reps, C.byref(v))
+        out[name] = v.value if st == 0 else None
+    return out
+
+
 def rel_err(got, ref):
     mask = ref > 1e-6 * ref.max()
     r = np.abs(got[mask] - ref[mask]) / ref[mask]
@@ -237,6 +251,11 @@ def run_gb300(args, ws, rank, local):
     stream = torch.cuda.current_stream(dev)
     r.set_stream(stream)
 
+    # footprint bins and block shape for this Nside, measured on a sample
+    from annmap import autotune
+    tuned = autotune.tune(r, dparts, nside, annmap.COMP_F32, sample=min(n, 1 << 21), reps=2,
+                          out=dmap)
+
     disc_ms, step_ms, step_stats = [], [], None
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     # the clock sampler starts before the warm-up so its start-up is not timed
@@ -270,7 +289,9 @@ def run_gb300(args, ws, rank, local):
                        "particles": n, "nside": nside,
                        "form": "compensated FP32 (FP64 geometry, FP32 weights, two-float sums)",
                        "parallelism": f"replicas x{ws}",
-                       "l2": "no flush: inputs 403 MB + map/planes 805 MB > 126 MB L2"},
+                       "l2": "no flush: inputs 403 MB + map/planes 805 MB > 126 MB L2",
+                       "tuning": dict(tuned["best"], autotune_s=round(tuned["seconds"], 2),
+                                      cached=tuned["cached"])},
             "clocks": clocks, "gpu_launches": KERNELS_PER_STEP * args.steps,
             "deposits_per_step": step_stats["deposits"],
             "deposits_per_s": step_stats["deposits"] / (ms / 1e3),
@@ -290,6 +311,16 @@ def run_gb300(args, ws, rank, local):
                         "traffic": traffic["dram_bytes_per_launch_scaled"] if traffic else None,
                         "algorithmic_bytes": alg_bytes,
                         "basis": "8 B per deposit (FP64 map read-modify-write) / disc-kernel time"}
+    # the deposit scatter against the L2 reduction rates measured here
+    l2 = measure_l2_red(local)
+    dep_rate = step_stats["deposits"] / (dms / 1e3)
+    line["roofline"]["l2_red"] = {
+        "achieved_ops": dep_rate, "unit": "reductions/s",
+        "peak_red_f32_ops": l2["red_f32"], "peak_comp_f32_ops": l2["comp_f32"],
+        "peak_red_f64_ops": l2["red_f64"],
+        "frac_red_f32": dep_rate / l2["red_f32"] if l2["red_f32"] else None,
+        "frac_comp_f32": dep_rate / l2["comp_f32"] if l2["comp_f32"] else None,
+        "basis": "deposits / disc-kernel time vs a coalesced sweep of reductions over 400 MB"}
 
     if not args.no_extras and rank == 0:
         # plain FP64 form on a prefix (the plain form is FP64-throughput bound)
@@ -340,6 +371,11 @@ def run_gb300(args, ws, rank, local):
                                     "kind": "port",
                                     "sample": f"{cpu['particles']} of {n} particles (shuffled prefix, "
                                               f"i.i.d.), {cpu['seconds']:.1f} s on {cpu['cores']} threads"}
+            # the reference's own loop is single-threaded (genmap.cpp:67-156)
+            cpu1, _, _, _ = cpu_oracle_run(P, nside, min(8.0, args.cpu_seconds), threads=1)
+            line["cpu_baseline_1thread"] = {"value": cpu1["value"], "unit": UNIT, "cores": 1,
+                                            "kind": "port", "sample": f"{cpu1['particles']} particles, "
+                                            f"{cpu1['seconds']:.1f} s on 1 thread"}
             r.set_stream(None)
             g = r.render(csub.as_dict(), nside, annmap.COMP_F32)
             med2, mx2 = rel_err(g, omap)
@@ -375,6 +411,8 @@ def bench_batched(dev):
     outs = [torch.empty(12 * ns * ns, dtype=torch.float64, device=dev) for ns in nsides]
     r = annmap.Renderer(dev.index or 0)
     r.set_params(par)
+    from annmap import autotune
+    tuned = autotune.tune_nsides(r, dparts, nsides, annmap.COMP_F32, sample=1 << 20, reps=1)
     r.render_batch(dparts, frames, nsides, annmap.COMP_F32, outs=outs)   # warm-up
     torch.cuda.synchronize()
     t0 = time.perf_counter()
@@ -385,7 +423,8 @@ def bench_batched(dev):
     return {"workload": "nfw8m_sub50_batched", "particles": len(P), "observers": len(obs),
             "nsides": sorted(set(nsides)), "form": "compensated FP32", "seconds": dt,
             "maps_per_s": len(obs) / dt, "particle_maps_per_s": len(P) * len(obs) / dt,
-            "launch": "one CUDA graph (dmann_render_batch, device maps)"}
+            "launch": "one CUDA graph (dmann_render_batch, device maps)",
+            "tuning": {str(k): v["best"] for k, v in tuned.items()}}
 
 
 def bench_adjoint(dev):

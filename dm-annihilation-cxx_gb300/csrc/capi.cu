@@ -49,6 +49,7 @@ struct dmann_ctx {
     double unit_factor = 1.0, hires = INFINITY;
     int flux_model = DMANN_FLUX_ANN_NOSOM;
     dmann_tuning tune{};
+    std::map<int, dmann_tuning> tune_ns;   // per-Nside overrides (the autotuner's table)
     std::map<int, RingTables> rings;
     // workspace
     DevBuf in[6], theta, phi, ar, flux, cpix, key, queue, hist, ctr, fsum, acc, map;
@@ -71,6 +72,19 @@ namespace {
 dmann_status fail(dmann_ctx *c, dmann_status s, const std::string &msg) {
     if (c) c->err = msg;
     return s;
+}
+
+// The tuning in force for maps of `nside`: its per-Nside entry, else the
+// context's default.
+const dmann_tuning &tuning_for(const dmann_ctx *ctx, int nside) {
+    auto it = ctx->tune_ns.find(nside);
+    return it != ctx->tune_ns.end() ? it->second : ctx->tune;
+}
+
+int block_bucket_min(const dmann_tuning &t) {
+    int bmin = 0;
+    while (bmin < kBuckets && (1LL << bmin) <= t.warp_max_pixels) bmin++;
+    return bmin;
 }
 
 #define CK(call)                                                                                  \
@@ -234,7 +248,7 @@ dmann_status dmann_create(dmann_ctx **out, int device) {
     ctx->tune.warp_max_pixels = 1024;
     ctx->tune.block_threads = 256;
     ctx->tune.blocks_per_sm = 0;
-    ctx->tune.ring_chunk = 256;
+    ctx->tune.ring_chunk = 384;
     *out = ctx;
     return DMANN_OK;
 }
@@ -319,16 +333,49 @@ dmann_status dmann_set_units(dmann_ctx *ctx, double unit_factor, double hires_th
     return DMANN_OK;
 }
 
+namespace {
+dmann_status merge_tuning(dmann_ctx *ctx, const dmann_tuning &t, dmann_tuning &dst) {
+    if (t.block_threads != 0 && t.block_threads != 128 && t.block_threads != 256 &&
+        t.block_threads != 512)
+        return fail(ctx, DMANN_ERR_INVALID, "block_threads must be 128, 256 or 512");
+    if (t.warp_max_pixels < 0 || t.blocks_per_sm < 0)
+        return fail(ctx, DMANN_ERR_INVALID, "negative tuning value");
+    if (t.warp_max_pixels > 0) dst.warp_max_pixels = t.warp_max_pixels;
+    if (t.blocks_per_sm > 0) dst.blocks_per_sm = t.blocks_per_sm;
+    if (t.block_threads > 0) dst.block_threads = t.block_threads;
+    dst.ring_chunk = dst.block_threads == 128 ? 192 : dst.block_threads == 512 ? 640 : 384;
+    return DMANN_OK;
+}
+}  // namespace
+
 dmann_status dmann_set_tuning(dmann_ctx *ctx, const dmann_tuning *t) {
     if (!ctx || !t) return DMANN_ERR_INVALID;
-    if (t->warp_max_pixels > 0) ctx->tune.warp_max_pixels = t->warp_max_pixels;
-    if (t->blocks_per_sm > 0) ctx->tune.blocks_per_sm = t->blocks_per_sm;
-    return DMANN_OK;
+    return merge_tuning(ctx, *t, ctx->tune);
 }
 
 dmann_status dmann_get_tuning(const dmann_ctx *ctx, dmann_tuning *t) {
     if (!ctx || !t) return DMANN_ERR_INVALID;
     *t = ctx->tune;
+    return DMANN_OK;
+}
+
+dmann_status dmann_set_tuning_nside(dmann_ctx *ctx, int nside, const dmann_tuning *t) {
+    if (!ctx) return DMANN_ERR_INVALID;
+    if (nside < 1 || nside > 8192) return fail(ctx, DMANN_ERR_INVALID, "nside must be in [1, 8192]");
+    if (!t) {
+        ctx->tune_ns.erase(nside);
+        return DMANN_OK;
+    }
+    dmann_tuning merged = ctx->tune;
+    dmann_status st = merge_tuning(ctx, *t, merged);
+    if (st != DMANN_OK) return st;
+    ctx->tune_ns[nside] = merged;
+    return DMANN_OK;
+}
+
+dmann_status dmann_get_tuning_nside(const dmann_ctx *ctx, int nside, dmann_tuning *t) {
+    if (!ctx || !t) return DMANN_ERR_INVALID;
+    *t = tuning_for(ctx, nside);
     return DMANN_OK;
 }
 
@@ -438,8 +485,8 @@ dmann_status dmann_map_add(dmann_ctx *ctx, const float *x, const float *y, const
     double scale;
     const Frame f = make_frame(ctx, &scale);
     const Accum acc = make_accum(ctx);
-    int bmin = 0;
-    while (bmin < kBuckets && (1LL << bmin) <= ctx->tune.warp_max_pixels) bmin++;
+    const dmann_tuning &tu = tuning_for(ctx, ctx->g.nside);
+    const int bmin = block_bucket_min(tu);
 
     CK(cudaMemsetAsync(ctx->hist.p, 0, 4 * (size_t)kKeys, s));
     CK(cudaMemsetAsync((long long *)ctx->ctr.p + kCtrChunkFirst, 0, 8 * (C_COUNT - kCtrChunkFirst), s));
@@ -473,8 +520,8 @@ dmann_status dmann_map_add(dmann_ctx *ctx, const float *x, const float *y, const
     da.ctr = pa.ctr;
     da.acc = acc;
     CK(cudaEventRecord(ctx->evd0, s));
-    if (ctx->precision == DMANN_PLAIN_F64) CK(launch_disc_plain(da, ctx->num_sms, ctx->tune.blocks_per_sm, s, ctx->evdm));
-    else CK(launch_disc_comp(da, ctx->num_sms, ctx->tune.blocks_per_sm, s, ctx->evdm));
+    if (ctx->precision == DMANN_PLAIN_F64) CK(launch_disc_plain(da, ctx->num_sms, tu.blocks_per_sm, s, ctx->evdm));
+    else CK(launch_disc_comp(da, ctx->num_sms, tu.blocks_per_sm, tu.block_threads, s, ctx->evdm));
     CK(cudaEventRecord(ctx->evd1, s));
     ctx->disc_timed = true;
     return DMANN_OK;
@@ -547,8 +594,8 @@ dmann_status issue_observer(dmann_ctx *ctx, const float *const dev[6], int n, in
     const Frame f = make_frame(ctx, &scale);
     const Accum acc = make_accum(ctx);
     if (n > 0) {
-        int bmin = 0;
-        while (bmin < kBuckets && (1LL << bmin) <= ctx->tune.warp_max_pixels) bmin++;
+        const dmann_tuning &tu = tuning_for(ctx, nside);
+        const int bmin = block_bucket_min(tu);
         CK(cudaMemsetAsync(ctx->hist.p, 0, 4 * (size_t)kKeys, s));
         PrepArgs pa;
         pa.p = {dev[0], dev[1], dev[2], dev[3], dev[4], dev[5], n};
@@ -578,8 +625,8 @@ dmann_status issue_observer(dmann_ctx *ctx, const float *const dev[6], int n, in
         da.queue = (const int *)ctx->queue.p;
         da.ctr = pa.ctr;
         da.acc = acc;
-        if (precision == DMANN_PLAIN_F64) CK(launch_disc_plain(da, ctx->num_sms, ctx->tune.blocks_per_sm, s, nullptr));
-        else CK(launch_disc_comp(da, ctx->num_sms, ctx->tune.blocks_per_sm, s, nullptr));
+        if (precision == DMANN_PLAIN_F64) CK(launch_disc_plain(da, ctx->num_sms, tu.blocks_per_sm, s, nullptr));
+        else CK(launch_disc_comp(da, ctx->num_sms, tu.blocks_per_sm, tu.block_threads, s, nullptr));
     }
     CK(launch_finalize(acc, precision, ctx->g.npix, ctx->g.dOmega, scale, dmap, 0, s));
     return DMANN_OK;
@@ -733,8 +780,7 @@ dmann_status dmann_adjoint(dmann_ctx *ctx, const float *x, const float *y, const
     }
     double scale;
     const Frame f = make_frame(ctx, &scale);
-    int bmin = 0;
-    while (bmin < kBuckets && (1LL << bmin) <= ctx->tune.warp_max_pixels) bmin++;
+    const int bmin = block_bucket_min(ctx->tune);
     CK(cudaEventRecord(ctx->ev0, s));
     CK(cudaMemsetAsync(ctx->ctr.p, 0, 8 * C_COUNT, s));
     CK(cudaMemsetAsync(ctx->fsum.p, 0, 8, s));

@@ -352,15 +352,16 @@ __device__ void render_particle(const DiscArgs &a, CompSmem<RCH> &sm, int pidx) 
     }
 }
 
-constexpr int kBT = 256, kRCH = 384;   // block kernel: 8 blocks x 24.6 KB of runs per SM
 constexpr int kWPB = 8, kRCHW = 64;    // warp kernel
 
-// One 256-thread block per large disc, persistent over the block-class queue
-// (largest discs first, claimed dynamically).  Eight resident blocks per SM
-// are asked of the compiler: the kernel is latency bound (returned atomics),
-// and full occupancy measured fastest.
-__global__ void __launch_bounds__(kBT, 8) k_comp_block(DiscArgs a) {
-    __shared__ CompSmem<kRCH> sm;
+// One block per large disc, persistent over the block-class queue (largest
+// discs first, claimed dynamically).  Block shapes: BT threads, runs of RCH
+// rings staged per chunk, MINB resident blocks per SM -- every shape fills
+// the SM with 2048 threads (the kernel is latency bound: returned atomics)
+// and about 200 KB of staged runs.  The autotuner picks the shape.
+template <int BT, int RCH, int MINB>
+__global__ void __launch_bounds__(BT, MINB) k_comp_block(DiscArgs a) {
+    __shared__ CompSmem<RCH> sm;
     __shared__ int s_q;
     const long long nblk = a.ctr[C_ADD_BLOCK];
     for (;;) {
@@ -369,7 +370,7 @@ __global__ void __launch_bounds__(kBT, 8) k_comp_block(DiscArgs a) {
         const int q = s_q;
         __syncthreads();
         if (q >= nblk) break;
-        render_particle<kBT, kRCH>(a, sm, a.queue[q]);
+        render_particle<BT, RCH>(a, sm, a.queue[q]);
     }
 }
 
@@ -384,17 +385,26 @@ __global__ void __launch_bounds__(kWPB * 32) k_comp_warp(DiscArgs a) {
     for (long long q = nblk + gw; q < ndisc; q += nw) render_particle<32, kRCHW>(a, sm[w], a.queue[q]);
 }
 
-}  // namespace
-
-cudaError_t launch_disc_comp(const DiscArgs &a, int num_sms, int blocks_per_sm, cudaStream_t s,
-                             cudaEvent_t mid) {
+template <int BT, int RCH, int MINB>
+cudaError_t launch_block(const DiscArgs &a, int num_sms, int blocks_per_sm, cudaStream_t s) {
     int occ = 0;
-    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_comp_block, kBT, 0);
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_comp_block<BT, RCH, MINB>, BT, 0);
     if (e != cudaSuccess) return e;
     int bps = blocks_per_sm > 0 ? min(blocks_per_sm, occ) : occ;
     if (bps < 1) bps = 1;
-    k_comp_block<<<num_sms * bps, kBT, 0, s>>>(a);
-    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    k_comp_block<BT, RCH, MINB><<<num_sms * bps, BT, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+cudaError_t launch_disc_comp(const DiscArgs &a, int num_sms, int blocks_per_sm, int block_threads,
+                             cudaStream_t s, cudaEvent_t mid) {
+    cudaError_t e;
+    if (block_threads == 128) e = launch_block<128, 192, 16>(a, num_sms, blocks_per_sm, s);
+    else if (block_threads == 512) e = launch_block<512, 640, 4>(a, num_sms, blocks_per_sm, s);
+    else e = launch_block<256, 384, 8>(a, num_sms, blocks_per_sm, s);
+    if (e != cudaSuccess) return e;
     if (mid && (e = cudaEventRecord(mid, s)) != cudaSuccess) return e;
     int occw = 0;
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occw, k_comp_warp, kWPB * 32, 0);

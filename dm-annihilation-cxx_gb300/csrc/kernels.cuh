@@ -83,8 +83,10 @@ cudaError_t launch_finalize(const Accum &acc, int precision, int npix, double dO
 // warp-per-particle kernel.
 cudaError_t launch_disc_plain(const DiscArgs &a, int num_sms, int blocks_per_sm, cudaStream_t s,
                               cudaEvent_t mid);
-cudaError_t launch_disc_comp(const DiscArgs &a, int num_sms, int blocks_per_sm, cudaStream_t s,
-                             cudaEvent_t mid);
+// block_threads: 128, 256 or 512 (the compensated block kernel's shape;
+// anything else means 256).
+cudaError_t launch_disc_comp(const DiscArgs &a, int num_sms, int blocks_per_sm, int block_threads,
+                             cudaStream_t s, cudaEvent_t mid);
 // adjoint.cu: gradients of the plain-form map for dL/dmap = gmap; grad is
 // [6][n] (x, y, z, m, rho, h); oacc[12] (zeroed by the caller) receives
 // sum_i dL/du_i and dL/drot (row-major).  Needs the prep outputs (with cls)

@@ -234,7 +234,7 @@ extern "C" dmann_status dmann_render_noalloc(const float *x, const float *y, con
         da.queue = (const int *)(b + L.queue);
         da.ctr = pa.ctr;
         da.acc = acc;
-        NA_CK(launch_disc_comp(da, sms, 0, s, nullptr));
+        NA_CK(launch_disc_comp(da, sms, 0, 256, s, nullptr));
     }
     NA_CK(launch_finalize(acc, DMANN_COMP_F32, npix, g.dOmega, scale, map_out, accumulate, s));
     return DMANN_OK;

@@ -59,6 +59,8 @@ SIGNATURES = {
     "dmann_set_units": (C.c_int, [_P, C.c_double, C.c_double, C.c_int]),
     "dmann_set_tuning": (C.c_int, [_P, C.POINTER(Tuning)]),
     "dmann_get_tuning": (C.c_int, [_P, C.POINTER(Tuning)]),
+    "dmann_set_tuning_nside": (C.c_int, [_P, C.c_int, C.POINTER(Tuning)]),
+    "dmann_get_tuning_nside": (C.c_int, [_P, C.c_int, C.POINTER(Tuning)]),
     "dmann_render": (C.c_int, [_P, _P, _P, _P, _P, _P, _P, C.c_int64, C.c_int, C.c_int, _P, C.c_int]),
     "dmann_map_begin": (C.c_int, [_P, C.c_int, C.c_int]),
     "dmann_map_add": (C.c_int, [_P, _P, _P, _P, _P, _P, _P, C.c_int64]),
@@ -67,6 +69,7 @@ SIGNATURES = {
     "dmann_render_batch": (C.c_int, [_P, _P, _P, _P, _P, _P, _P, C.c_int64, C.c_int, _D3, _D3,
                                      C.POINTER(C.c_int), C.c_int, C.POINTER(C.c_void_p)]),
     "dmann_adjoint": (C.c_int, [_P, _P, _P, _P, _P, _P, _P, C.c_int64, C.c_int, _P, _P, _D3]),
+    "dmann_measure_l2_red": (C.c_int, [C.c_int, C.c_int, C.c_int64, C.c_int, _D3]),
     "dmann_observer_rotation": (C.c_int, [_D3, _D3, _D3, _D3, _D3]),
     "dmann_observer_rotation_jacobian": (C.c_int, [_D3, _D3, _D3, _D3]),
     "dmann_code_units": (C.c_int, [C.c_double, C.c_double, C.c_double, _D3]),

@@ -101,15 +101,26 @@ class Renderer:
         self.set_frame(par.rotmatrix, par.params.opos)
         self.set_units(par.unit_factor, par.hires_threshold)
 
-    def set_tuning(self, **kw):
+    def set_tuning(self, nside: int | None = None, **kw):
+        """Default tuning, or the entry for maps of ``nside``
+        (warp_max_pixels, block_threads, blocks_per_sm)."""
         t = _lib.Tuning()
         for k, v in kw.items():
             setattr(t, k, v)
-        self._check(self.L.dmann_set_tuning(self.ctx, C.byref(t)))
+        if nside is None:
+            self._check(self.L.dmann_set_tuning(self.ctx, C.byref(t)))
+        else:
+            self._check(self.L.dmann_set_tuning_nside(self.ctx, int(nside), C.byref(t)))
 
-    def get_tuning(self) -> dict:
+    def clear_tuning(self, nside: int):
+        self._check(self.L.dmann_set_tuning_nside(self.ctx, int(nside), None))
+
+    def get_tuning(self, nside: int | None = None) -> dict:
         t = _lib.Tuning()
-        self._check(self.L.dmann_get_tuning(self.ctx, C.byref(t)))
+        if nside is None:
+            self._check(self.L.dmann_get_tuning(self.ctx, C.byref(t)))
+        else:
+            self._check(self.L.dmann_get_tuning_nside(self.ctx, int(nside), C.byref(t)))
         return {k: getattr(t, k) for k, _ in _lib.Tuning._fields_ if k != "reserved"}
 
     # ------------------------------------------------------------ rendering

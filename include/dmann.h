@@ -93,12 +93,19 @@ typedef struct {
     double total_flux;     /* sum of kept flux (before the dOmega division) */
 } dmann_stats;
 
-/* Tunables (an autotuner may set them; zero fields keep defaults). */
+/* Tunables (set by the annmap autotuner; zero fields keep the current
+ * values).  Defaults: warp_max_pixels 1024, block_threads 256, blocks_per_sm
+ * 0 (as many as fit). */
 typedef struct {
-    int64_t warp_max_pixels;   /* discs up to this estimate go warp-per-particle */
-    int32_t block_threads;     /* threads of the block-per-particle kernel */
-    int32_t blocks_per_sm;     /* resident blocks per SM for persistent kernels */
-    int32_t ring_chunk;        /* rings staged in shared memory per pass */
+    int64_t warp_max_pixels;   /* footprint-class bin edge: discs estimated up
+                                  to this many pixels go warp-per-particle,
+                                  larger ones block-per-particle */
+    int32_t block_threads;     /* compensated block kernel shape: 128, 256 or
+                                  512 threads (the plain form always uses 256) */
+    int32_t blocks_per_sm;     /* resident blocks per SM of the persistent
+                                  block kernel, capped by occupancy; 0 = max */
+    int32_t ring_chunk;        /* read only: rings staged per pass for the
+                                  block shape (192, 384, 640) */
     int32_t reserved[3];
 } dmann_tuning;
 
@@ -128,8 +135,16 @@ dmann_status dmann_set_frame(dmann_ctx *ctx, const double rot[9],
  * reference; pass INFINITY to keep every particle). */
 dmann_status dmann_set_units(dmann_ctx *ctx, double unit_factor,
                              double hires_threshold, int flux_model);
+/* The context's default tuning (DMANN_ERR_INVALID for a block shape other
+ * than 128/256/512 or negative values). */
 dmann_status dmann_set_tuning(dmann_ctx *ctx, const dmann_tuning *t);
 dmann_status dmann_get_tuning(const dmann_ctx *ctx, dmann_tuning *t);
+/* Per-Nside tuning: maps of this nside (dmann_render, the streaming calls
+ * and each observer of dmann_render_batch) use this entry instead of the
+ * default; zero fields take the default's current values.  t = NULL removes
+ * the entry.  dmann_get_tuning_nside returns the tuning in force for nside. */
+dmann_status dmann_set_tuning_nside(dmann_ctx *ctx, int nside, const dmann_tuning *t);
+dmann_status dmann_get_tuning_nside(const dmann_ctx *ctx, int nside, dmann_tuning *t);
 
 /* ---- rendering ---- */
 /* Projects n particles (float32 SoA: positions x,y,z, mass m, density rho,
@@ -227,6 +242,23 @@ dmann_status dmann_render_noalloc(const float *x, const float *y, const float *z
                                   const double opos[3], double unit_factor,
                                   double hires_threshold, double *map_out,
                                   int accumulate, void *stream);
+
+/* ---- diagnostics ---- */
+/* Reduction kinds of dmann_measure_l2_red. */
+typedef enum {
+    DMANN_PEAK_RED_F32 = 0,   /* red.global.add.f32 */
+    DMANN_PEAK_RED_F64 = 1,   /* red.global.add.f64 */
+    DMANN_PEAK_COMP_F32 = 2   /* the compensated deposit: returning FP32 atomic
+                                 add, exact TwoSum error, FP32 red of the error */
+} dmann_peak_kind;
+/* No reference counterpart.  Measures the rate (operations per second) of
+ * one kind of global reduction on `device`: a grid of 8 blocks per SM sweeps
+ * an array of `bytes` (1 MiB .. 16 GiB; a 400 MB array exceeds the L2) with
+ * lanes of a warp on consecutive elements, `reps` times, after one warm-up
+ * sweep.  The deposit scatter of the projection is bound by this rate (one
+ * reduction per algorithmic deposit). */
+dmann_status dmann_measure_l2_red(int device, int kind, int64_t bytes, int reps,
+                                  double *ops_per_s);
 
 /* ---- host-only helpers (no context, no GPU) ---- */
 /* Parameters::setupParams + setupRotation (src/parameters.cpp:111-152,
