@@ -51,6 +51,7 @@ def parse():
     ap.add_argument("--plain-scale", type=float, default=1.0 / 64)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-extras", action="store_true", help="skip plain form, e2e and CPU legs")
+    ap.add_argument("--no-tune", action="store_true", help="keep the default tuning (no autotuner)")
     return ap.parse_args()
 
 
@@ -253,8 +254,11 @@ def run_gb300(args, ws, rank, local):
 
     # footprint bins and block shape for this Nside, measured on a sample
     from annmap import autotune
-    tuned = autotune.tune(r, dparts, nside, annmap.COMP_F32, sample=min(n, 1 << 21), reps=2,
-                          out=dmap)
+    if args.no_tune:
+        tuned = {"best": r.get_tuning(), "seconds": 0.0, "cached": False}
+    else:
+        tuned = autotune.tune(r, dparts, nside, annmap.COMP_F32, sample=min(n, 1 << 21), reps=2,
+                              out=dmap)
 
     disc_ms, step_ms, step_stats = [], [], None
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
