@@ -28,6 +28,7 @@ struct DevBuf {
 
 struct RingTables {
     double *z = nullptr, *st = nullptr, *theta = nullptr, *step = nullptr;
+    float *st32 = nullptr, *step32 = nullptr;
 };
 
 }  // namespace
@@ -181,6 +182,15 @@ dmann_status ring_tables(dmann_ctx *ctx, int nside, RingTables &out) {
     CK(cudaMemcpy(t.theta, th.data(), sizeof(double) * n, cudaMemcpyHostToDevice));
     CK(cudaMalloc(&t.step, sizeof(double) * n));
     CK(cudaMemcpy(t.step, stp.data(), sizeof(double) * n, cudaMemcpyHostToDevice));
+    std::vector<float> st32(n), stp32(n);
+    for (int r = 0; r < n; r++) {
+        st32[r] = (float)st[r];
+        stp32[r] = (float)stp[r];
+    }
+    CK(cudaMalloc(&t.st32, sizeof(float) * n));
+    CK(cudaMemcpy(t.st32, st32.data(), sizeof(float) * n, cudaMemcpyHostToDevice));
+    CK(cudaMalloc(&t.step32, sizeof(float) * n));
+    CK(cudaMemcpy(t.step32, stp32.data(), sizeof(float) * n, cudaMemcpyHostToDevice));
     ctx->rings[nside] = t;
     out = t;
     return DMANN_OK;
@@ -268,6 +278,8 @@ void dmann_destroy(dmann_ctx *ctx) {
         cudaFree(kv.second.st);
         cudaFree(kv.second.theta);
         cudaFree(kv.second.step);
+        cudaFree(kv.second.st32);
+        cudaFree(kv.second.step32);
     }
     if (ctx->h_ctr) cudaFreeHost(ctx->h_ctr);
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
@@ -510,7 +522,7 @@ dmann_status dmann_map_add(dmann_ctx *ctx, const float *x, const float *y, const
     DiscArgs da;
     da.g = ctx->g;
     da.f = f;
-    da.rt = {ctx->rt.z, ctx->rt.st, ctx->rt.theta, ctx->rt.step};
+    da.rt = {ctx->rt.z, ctx->rt.st, ctx->rt.theta, ctx->rt.step, ctx->rt.st32, ctx->rt.step32};
     da.theta = pa.out.theta;
     da.phi = pa.out.phi;
     da.ar = pa.out.ar;
@@ -616,7 +628,7 @@ dmann_status issue_observer(dmann_ctx *ctx, const float *const dev[6], int n, in
         DiscArgs da;
         da.g = ctx->g;
         da.f = f;
-        da.rt = {rt.z, rt.st, rt.theta, rt.step};
+        da.rt = {rt.z, rt.st, rt.theta, rt.step, rt.st32, rt.step32};
         da.theta = pa.out.theta;
         da.phi = pa.out.phi;
         da.ar = pa.out.ar;
@@ -806,7 +818,7 @@ dmann_status dmann_adjoint(dmann_ctx *ctx, const float *x, const float *y, const
     DiscArgs da;
     da.g = g;
     da.f = f;
-    da.rt = {rt.z, rt.st, rt.theta, rt.step};
+    da.rt = {rt.z, rt.st, rt.theta, rt.step, rt.st32, rt.step32};
     da.theta = pa.out.theta;
     da.phi = pa.out.phi;
     da.ar = pa.out.ar;

@@ -45,6 +45,8 @@ struct RingTab {
     const double *st;
     const double *theta;
     const double *step;   // 2 pi / (pixels in the ring)
+    const float *st32;    // st and step rounded to FP32 (the compensated form's
+    const float *step32;  // per-ring set-up runs in FP32 where it can)
 };
 
 __host__ __device__ inline int64_t ring_start(const Hpx &g, int ring) {

@@ -63,7 +63,8 @@ struct alignas(16) Run {
     int pix0, cnt;
     float A, B;         // hav(theta_r - theta0), sin(theta_r) sin(theta0)
     float d0h, steph;   // half azimuth offset of pixel 0, half the pixel step
-    float A2, pad;      // hav(theta_r + theta0 - pi): distance to the antipode
+    float A2;           // hav(theta_r + theta0 - pi): distance to the antipode
+    int more;           // the ring continues in the next run slot (it wrapped)
 };
 
 struct Ext {
@@ -71,17 +72,27 @@ struct Ext {
     int small_h, small_x;
 };
 
+// Per-particle constants of the FP32 chord test (see chord_fast).
+struct Chord {
+    float hR;           // hav(R) = sin^2(R/2), R the disc radius
+    float sth0;         // sin(theta0)
+    int ci[2];          // c = nr/(2 pi) phi0 - shift for the equatorial rings
+    float cf[2];        // (nr = 4 nside), shift 0 and 1/2: floor(c) and c - floor(c)
+    int fast;           // the FP32 test may be used for this particle
+};
+
 template <int RCH>
 struct CompSmem {
     Run run[2 * RCH];   // two runs per ring (the second only where it wraps)
     DiscHdr hdr;
     Ext ext;
+    Chord ch;
     double red[32];
     int cnt_red[32];
     int next_run;       // runs claimed so far in the current pass (block groups)
 };
 
-__device__ inline void particle_setup(const DiscHdr &d, Ext &e) {
+__device__ inline void particle_setup(const Hpx &g, const DiscHdr &d, Ext &e, Chord &ch) {
     e.nK = -(float)(4.0 * 1.4426950408889634 * 0.5 / (0.333 * d.ar * d.ar));
     double hmax = 1.0;
     if (!d.allsky) {
@@ -89,6 +100,16 @@ __device__ inline void particle_setup(const DiscHdr &d, Ext &e) {
         hmax = s * s;
     }
     e.small_h = hmax < 0.02;
+    ch.hR = (float)hmax;
+    ch.sth0 = (float)d.sth0;
+    ch.fast = !d.allsky && d.sth0 > 1e-3;
+    const double fnr = __dmul_rn((double)(4 * g.nside), kInvTwoPi);
+    for (int k = 0; k < 2; k++) {
+        const double c = __dsub_rn(__dmul_rn(fnr, d.phi0), k ? 0.5 : 0.0);
+        const double fl = floor(c);
+        ch.ci[k] = (int)fl;
+        ch.cf[k] = (float)(c - fl);
+    }
     const bool caps = d.allsky || d.r_first < d.irmin || d.r_last > d.irmax;
     int small_x = 0;
     if (!caps) {
@@ -98,27 +119,117 @@ __device__ inline void particle_setup(const DiscHdr &d, Ext &e) {
     e.small_x = small_x;
 }
 
+__device__ inline bool near_int_f(float a, float tau) {
+    const float fr = a - floorf(a);
+    return fr < tau || fr > 1.0f - tau;
+}
+
+// The chord of ring `ring` in FP32.  With q = sin^2(dphi/2), where dphi is
+// the half-width of the in-disc azimuth interval,
+//     q = (hav(R) - hav(theta_r - theta0)) / (sin theta_r sin theta0)
+// (the haversine form of query_disc's x = (cos R - z z0) / sin theta0,
+// ysq = 1 - z^2 - x^2 = 4 sin^2(theta_r) q (1 - q), dphi = atan2(sqrt(ysq), x)),
+// which stays well conditioned for small discs, where ysq is a difference of
+// numbers near 1.  The end points fnr (phi0 -+ dphi) - shift are formed as
+// c -+ fnr dphi with c = fnr phi0 - shift split into floor(c) + frac (FP64,
+// once per particle for the equatorial rings).  A running error bound covers
+// the FP32 roundings (inputs, sinf, asinf, sqrtf: a few ulp each) and the
+// rounding of the FP64 form this must reproduce; when an end point lies
+// within the bound of an integer, or q is too close to 0 or 1 to decide, the
+// caller takes the exact FP64 test instead.  So the pixel runs are those of
+// the exact test.  Returns false for "undecided".
+__device__ inline bool chord_fast(const Hpx &g, const DiscHdr &d, const Chord &ch, int ring, int nr,
+                                  bool shifted, float A, float st32, int &ip_lo, int &ip_hi, int &ci,
+                                  float &cf) {
+    if (!(st32 > 0.01f)) return false;
+    const float B = st32 * ch.sth0;
+    const float num = ch.hR - A;
+    const float dnum = 1.2e-7f * ch.hR + 8e-7f * A + 1.2e-7f * fabsf(num);
+    if (num < -4.0f * dnum && -num > 1e-9f * B) {   // clearly outside: no pixel
+        ip_lo = 1;
+        ip_hi = 0;
+        ci = 0;
+        cf = 0.0f;
+        return true;
+    }
+    if (!(num > 4.0f * dnum)) return false;
+    const float q = __fdiv_rn(num, B);
+    const float eq = __fdiv_rn(dnum, num) + 4.2e-7f;   // relative error of q
+    if (!(q < 0.9999f) || eq > 1e-3f) return false;
+    const float sq = sqrtf(q);
+    const float dphi = 2.0f * asinf(sq);
+    // FP32 error of dphi (d dphi / dq = 1 / sqrt(q (1 - q))), doubled, plus
+    // the FP64 form's own rounding (ysq and x carry ~1e-16 absolute errors)
+    const float ddphi = 2.0f * (eq * sq * rsqrtf(1.0f - q) + 6e-7f * dphi) +
+                        1e-15f * (1.0f / (B * sq) + 1.0f / (st32 * st32 * sq)) + 1e-12f;
+    if (ring >= g.nside && ring <= 3 * g.nside) {
+        const int k = shifted ? 1 : 0;
+        ci = ch.ci[k];
+        cf = ch.cf[k];
+    } else {
+        const double fnr = __dmul_rn((double)nr, kInvTwoPi);
+        const double c = __dsub_rn(__dmul_rn(fnr, d.phi0), shifted ? 0.5 : 0.0);
+        const double fl = floor(c);
+        ci = (int)fl;
+        cf = (float)(c - fl);
+    }
+    const float fnr32 = (float)nr * 0.159154943091895336f;
+    const float w = fnr32 * dphi;
+    const float tau = fnr32 * ddphi + 2.4e-7f * w + 1.2e-7f * (1.0f + w) + 1e-6f;
+    const float xlo = cf - w, xhi = cf + w;
+    if (near_int_f(xlo, tau) || near_int_f(xhi, tau)) return false;
+    ip_lo = ci + (int)floorf(xlo) + 1;
+    ip_hi = ci + (int)floorf(xhi);
+    return true;
+}
+
 // Stages ring `ring` as run(s) run[0], run[1]; returns its pixel count.
-__device__ inline int make_runs(const DiscArgs &a, const DiscHdr &d, int ring, Run *run) {
-    int lo, cnt;
-    ring_segment_t<true>(a.g, d, ring, lo, cnt);
+__device__ inline int make_runs(const DiscArgs &a, const DiscHdr &d, const Chord &ch, bool need_a2,
+                                int ring, Run *run) {
     run[0].cnt = 0;
     run[1].cnt = 0;
-    if (cnt <= 0) return 0;
     const int start = (int)ring_start(a.g, ring);
     const int nr = ring_npix(a.g, ring);
-    const double shift = ring_shifted(a.g, ring) ? 0.5 : 0.0;
-    const double step = a.rt.step[ring];
+    const bool shifted = ring_shifted(a.g, ring);
     const double th = a.rt.theta[ring];
     const float sa = sinf(0.5f * (float)(th - d.theta0));
-    const float sb = sinf(0.5f * (float)(th + d.theta0 - kPi));
-    const float A = sa * sa, A2 = sb * sb;
-    const float B = (float)(a.rt.st[ring] * d.sth0);
-    const float steph = (float)(0.5 * step);
-    // azimuth of the first pixel relative to the particle, in [-pi, pi)
-    double d0 = ((double)lo + shift) * step - d.phi0;
-    if (d0 < -kPi) d0 += kTwoPi;
-    if (d0 >= kPi) d0 -= kTwoPi;
+    const float A = sa * sa;
+    float A2 = 0.0f;
+    if (need_a2) {
+        const float sb = sinf(0.5f * (float)(th + d.theta0 - kPi));
+        A2 = sb * sb;
+    }
+    const float st32 = a.rt.st32[ring];
+    const float B = st32 * ch.sth0;
+    const float step32 = a.rt.step32[ring];
+    const float steph = 0.5f * step32;
+    int lo, cnt;
+    float d0h;
+    int ip_lo, ip_hi, ci;
+    float cf;
+    const bool chord = !(d.allsky || ring < d.irmin || ring > d.irmax);
+    if (chord && ch.fast && chord_fast(a.g, d, ch, ring, nr, shifted, A, st32, ip_lo, ip_hi, ci, cf)) {
+        if (ip_lo > ip_hi) return 0;
+        // azimuth of pixel ip_lo relative to the particle: step (ip_lo - c),
+        // in (-dphi, -dphi + step]
+        d0h = 0.5f * fmaf(step32, (float)(ip_lo - ci), -step32 * cf);
+        if (ip_hi >= nr) {
+            ip_lo -= nr;
+            ip_hi -= nr;
+        }
+        lo = ip_lo;
+        cnt = ip_hi - ip_lo + 1;
+        if (cnt > nr || lo < -nr || lo >= nr) return 0;  // cannot happen for finite input
+    } else {
+        ring_segment_t<true>(a.g, d, ring, lo, cnt);
+        if (cnt <= 0) return 0;
+        const double shift = shifted ? 0.5 : 0.0;
+        // azimuth of the first pixel relative to the particle, in [-pi, pi)
+        double d0 = ((double)lo + shift) * a.rt.step[ring] - d.phi0;
+        if (d0 < -kPi) d0 += kTwoPi;
+        if (d0 >= kPi) d0 -= kTwoPi;
+        d0h = (float)(0.5 * d0);
+    }
     // split where the in-ring index wraps (lo < 0 or lo + cnt > nr)
     int c0 = cnt, p0 = start + lo;
     if (lo < 0) {
@@ -127,10 +238,10 @@ __device__ inline int make_runs(const DiscArgs &a, const DiscHdr &d, int ring, R
     } else if (lo + cnt > nr) {
         c0 = nr - lo;
     }
-    run[0] = Run{p0, c0, A, B, (float)(0.5 * d0), steph, A2, 0.0f};
+    run[0] = Run{p0, c0, A, B, d0h, steph, A2, c0 < cnt};
     if (c0 < cnt) {
         // the rest continues at the ring's first pixel, azimuth continuing
-        run[1] = Run{start, cnt - c0, A, B, (float)(0.5 * (d0 + (double)c0 * step)), steph, A2, 0.0f};
+        run[1] = Run{start, cnt - c0, A, B, fmaf((float)c0, steph, d0h), steph, A2, 0};
     }
     return cnt;
 }
@@ -212,7 +323,8 @@ template <int G, int RCH>
 __device__ inline int build_runs(const DiscArgs &a, CompSmem<RCH> &sm, int r0, int n) {
     using Gp = Grp<G>;
     int c = 0;
-    for (int i = Gp::rank(); i < n; i += G) c += make_runs(a, sm.hdr, r0 + i, &sm.run[2 * i]);
+    const bool need_a2 = !sm.ext.small_h;
+    for (int i = Gp::rank(); i < n; i += G) c += make_runs(a, sm.hdr, sm.ch, need_a2, r0 + i, &sm.run[2 * i]);
     c = __reduce_add_sync(0xffffffffu, c);
     if (G > 32) {
         if ((threadIdx.x & 31) == 0) sm.cnt_red[Gp::warp()] = c;
@@ -224,28 +336,36 @@ __device__ inline int build_runs(const DiscArgs &a, CompSmem<RCH> &sm, int r0, i
     return c;
 }
 
-// Walks the staged runs; lane l handles pixels l and l + 32 of each 64-pixel
-// stretch of a run.  body(run, j, second) gets the first pixel index j and
-// whether j + 32 is inside the run.  In a block, warps claim runs one at a
-// time from a shared counter (reset by the caller), so no warp waits at the
-// next barrier for more than about one run: ring runs differ a lot in length.
+// Walks the staged rings; lane l handles pixels l and l + 32 of each
+// 64-pixel stretch of a run.  body(run, j, second) gets the first pixel index
+// j and whether j + 32 is inside the run.  In a block, warps claim whole
+// rings (both run slots: the second only when the ring wrapped) from a shared
+// counter reset by the caller; the next claim is issued before the current
+// ring is walked, so its latency is hidden, and no warp waits at the next
+// barrier for more than about one ring.
 template <int G, int RCH, class Body>
 __device__ inline void run_walk(CompSmem<RCH> &sm, int n, Body body) {
     const int lane = threadIdx.x & 31;
-    if (G == 32) {
-        for (int q = 0; q < 2 * n; q++) {
-            const Run r = sm.run[q];
-            for (int j = lane; j < r.cnt; j += 64) body(r, j, j + 32 < r.cnt);
+    auto ring = [&](int i) {
+        const Run r = sm.run[2 * i];
+        for (int j = lane; j < r.cnt; j += 64) body(r, j, j + 32 < r.cnt);
+        if (r.more) {
+            const Run r2 = sm.run[2 * i + 1];
+            for (int j = lane; j < r2.cnt; j += 64) body(r2, j, j + 32 < r2.cnt);
         }
+    };
+    if (G == 32) {
+        for (int i = 0; i < n; i++) ring(i);
         return;
     }
-    for (;;) {
-        int q = 0;
-        if (lane == 0) q = atomicAdd(&sm.next_run, 1);
-        q = __shfl_sync(0xffffffffu, q, 0);
-        if (q >= 2 * n) break;
-        const Run r = sm.run[q];
-        for (int j = lane; j < r.cnt; j += 64) body(r, j, j + 32 < r.cnt);
+    int q = 0;
+    if (lane == 0) q = atomicAdd(&sm.next_run, 1);
+    q = __shfl_sync(0xffffffffu, q, 0);
+    while (q < n) {
+        int qn = 0;
+        if (lane == 0) qn = atomicAdd(&sm.next_run, 1);
+        ring(q);
+        q = __shfl_sync(0xffffffffu, qn, 0);
     }
 }
 
@@ -257,7 +377,7 @@ __device__ void render_particle(const DiscArgs &a, CompSmem<RCH> &sm, int pidx) 
     if (rk == 0) {
         disc_setup(a.g, a.theta[pidx], a.phi[pidx], a.ar[pidx], a.flux[pidx], a.cpix[pidx], pidx,
                    sm.hdr);
-        particle_setup(sm.hdr, sm.ext);
+        particle_setup(a.g, sm.hdr, sm.ext, sm.ch);
     }
     Gp::sync();
     const Ext e = sm.ext;

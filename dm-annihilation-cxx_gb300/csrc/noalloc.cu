@@ -27,11 +27,12 @@ int g_num_sms[kMaxDevices];
 
 // Per-ring tables, with the formulas of the context path's host tables.
 __global__ void k_ring_tables(int nside, double fact1, double fact2, double *z, double *st,
-                              double *th, double *step) {
+                              double *th, double *step, float *st32, float *step32) {
     const int n = 4 * nside;
     for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
         if (r == 0) {
             z[0] = st[0] = th[0] = step[0] = 0.0;
+            st32[0] = step32[0] = 0.0f;
             continue;
         }
         bool have = false;
@@ -58,6 +59,8 @@ __global__ void k_ring_tables(int nside, double fact1, double fact2, double *z, 
         st[r] = s;
         th[r] = have ? atan2(s, zz) : acos(zz);
         step[r] = __ddiv_rn(kTwoPi, (double)nr);
+        st32[r] = (float)s;
+        step32[r] = (float)step[r];
     }
 }
 
@@ -72,7 +75,7 @@ Layout layout(size_t n, int nside) {
     Layout L;
     const size_t npix = 12 * (size_t)nside * (size_t)nside;
     size_t o = 0;
-    L.ring = o;  o = up256(o + 4 * sizeof(double) * 4 * (size_t)nside);
+    L.ring = o;  o = up256(o + (4 * sizeof(double) + 2 * sizeof(float)) * 4 * (size_t)nside);
     L.hist = o;  o = up256(o + sizeof(int) * (size_t)kKeys);
     L.ctr = o;   o = up256(o + sizeof(long long) * C_COUNT);
     L.fsum = o;  o = up256(o + sizeof(double));
@@ -167,6 +170,7 @@ extern "C" dmann_status dmann_render_noalloc(const float *x, const float *y, con
     const int npix = 12 * nside * nside;
     double *rz = (double *)(b + L.ring), *rst = rz + 4 * nside, *rth = rst + 4 * nside,
            *rstep = rth + 4 * nside;
+    float *rst32 = (float *)(rstep + 4 * nside), *rstep32 = rst32 + 4 * nside;
 
     Hpx g;
     g.nside = nside;
@@ -202,7 +206,7 @@ extern "C" dmann_status dmann_render_noalloc(const float *x, const float *y, con
     NA_CK(cudaMemsetAsync(b + L.fsum, 0, sizeof(double), s));
     NA_CK(cudaMemsetAsync(b + L.acc, 0, 2 * sizeof(float) * (size_t)npix, s));
     k_ring_tables<<<(4 * nside + 255) / 256, 256, 0, s>>>(nside, g.fact1, g.fact2, rz, rst, rth,
-                                                          rstep);
+                                                          rstep, rst32, rstep32);
     NA_CK(cudaGetLastError());
 
     if (n > 0) {
@@ -225,7 +229,7 @@ extern "C" dmann_status dmann_render_noalloc(const float *x, const float *y, con
         DiscArgs da;
         da.g = g;
         da.f = f;
-        da.rt = {rz, rst, rth, rstep};
+        da.rt = {rz, rst, rth, rstep, rst32, rstep32};
         da.theta = pa.out.theta;
         da.phi = pa.out.phi;
         da.ar = pa.out.ar;

@@ -228,7 +228,7 @@ dmann_status dmann_get_stats(const dmann_ctx *ctx, dmann_stats *out);
  * dmann_set_frame and dmann_set_units take.  Work is queued on `stream`
  * (a cudaStream_t, NULL = the default stream) of the current device and the
  * call returns without waiting.  The scratch needed is about
- *     8 * 12*nside^2 + 44 * n + 128 * nside + 513 KiB   bytes;
+ *     8 * 12*nside^2 + 44 * n + 160 * nside + 513 KiB   bytes;
  * a larger problem is rejected with DMANN_ERR_TOO_LARGE (render it in chunks
  * of particles with accumulate = 1).  The first call on a device looks up the
  * array's device address (cudaGetSymbolAddress); make that first call before
