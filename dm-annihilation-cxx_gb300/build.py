@@ -38,6 +38,12 @@ LIB_DMANN = os.path.join(PKG, "libdmann.so")
 LIB_ANNMAP = os.path.join(PKG, "libannmap.so")
 
 
+def _cuda_home():
+    import shutil
+    nv = shutil.which(NVCC) or "/usr/local/cuda/bin/nvcc"
+    return os.path.dirname(os.path.dirname(os.path.realpath(nv)))
+
+
 def _headers():
     return (glob.glob(os.path.join(CSRC, "*.cuh")) + glob.glob(os.path.join(CSRC, "*.h")) +
             glob.glob(os.path.join(REPO, "include", "*.h")) + glob.glob(os.path.join(HOST, "*.hpp")))
@@ -86,9 +92,12 @@ def build(force: bool = False, verbose: bool = False) -> str:
         _run([NVCC] + ARCH + ["-shared", "-cudart", "shared", "-o", LIB_DMANN] + objs)
     host_srcs = sorted(glob.glob(os.path.join(HOST, "*.cpp")))
     if host_srcs and (force or _stale(LIB_ANNMAP, host_srcs + hdrs + [LIB_DMANN])):
+        cuda = _cuda_home()
         _run([CXX, "-O2", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off", "-Wall",
-              "-I" + os.path.join(REPO, "include"), "-I" + CSRC] + host_srcs +
-             ["-L" + PKG, "-ldmann", "-Wl,-rpath,$ORIGIN", "-o", LIB_ANNMAP])
+              "-I" + os.path.join(REPO, "include"), "-I" + HOST, "-I" + os.path.join(cuda, "include")] +
+             host_srcs + ["-L" + PKG, "-ldmann", "-L" + os.path.join(cuda, "lib64"), "-lcudart",
+                          "-Wl,-rpath,$ORIGIN", "-Wl,-rpath," + os.path.join(cuda, "lib64"),
+                          "-o", LIB_ANNMAP])
     return LIB_DMANN
 
 
