@@ -35,10 +35,10 @@ def test_cpp_genmap_matches_golden(tmp_path, name, buf, precision):
 
 
 def test_cpp_genmap_chunking_is_linear(tmp_path):
-    a, info_a = write_case(tmp_path / "a" if os.makedirs(tmp_path / "a") is None else None,
-                           "nfw_sub_ns64", mem_buffer=10000000)
-    b, info_b = write_case(tmp_path / "b" if os.makedirs(tmp_path / "b") is None else None,
-                           "nfw_sub_ns64", mem_buffer=97)
+    os.makedirs(tmp_path / "a")
+    os.makedirs(tmp_path / "b")
+    _, info_a = write_case(tmp_path / "a", "nfw_sub_ns64", mem_buffer=10000000)
+    _, info_b = write_case(tmp_path / "b", "nfw_sub_ns64", mem_buffer=97)
     ma, ta = host.genmap(info_a, COMP)
     mb, tb = host.genmap(info_b, COMP)
     m = ma > 0
