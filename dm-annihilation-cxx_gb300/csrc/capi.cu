@@ -49,11 +49,12 @@ struct dmann_ctx {
     double cpos[3] = {0, 0, 0}, align[3] = {0, 0, 0};
     double unit_factor = 1.0, hires = INFINITY;
     int flux_model = DMANN_FLUX_ANN_NOSOM;
+    double vel_to_cgs = 0.0, fcpos[3] = {0, 0, 0};   // dmann_set_flux_params
     dmann_tuning tune{};
     std::map<int, dmann_tuning> tune_ns;   // per-Nside overrides (the autotuner's table)
     std::map<int, RingTables> rings;
     // workspace
-    DevBuf in[6], theta, phi, ar, flux, cpix, key, queue, hist, ctr, fsum, acc, map;
+    DevBuf in[7], theta, phi, ar, flux, cpix, key, queue, hist, ctr, fsum, acc, map;
     DevBuf cls, oacc, grad;   // the adjoint's class array, observer sums, staged gradient
     dmann_stats stats{};
     bool stats_pending = false;
@@ -268,6 +269,7 @@ void dmann_destroy(dmann_ctx *ctx) {
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
     DevBuf *bufs[] = {&ctx->in[0], &ctx->in[1], &ctx->in[2], &ctx->in[3], &ctx->in[4], &ctx->in[5],
+                      &ctx->in[6],
                       &ctx->theta, &ctx->phi, &ctx->ar, &ctx->flux, &ctx->cpix, &ctx->key,
                       &ctx->queue, &ctx->hist, &ctx->ctr, &ctx->fsum, &ctx->acc, &ctx->map,
                       &ctx->cls, &ctx->oacc, &ctx->grad};
@@ -337,7 +339,8 @@ dmann_status dmann_set_units(dmann_ctx *ctx, double unit_factor, double hires_th
     if (!ctx) return DMANN_ERR_INVALID;
     if (!(std::isfinite(unit_factor) && unit_factor > 0))
         return fail(ctx, DMANN_ERR_INVALID, "unit_factor must be finite and positive");
-    if (flux_model != DMANN_FLUX_ANN_NOSOM) return fail(ctx, DMANN_ERR_INVALID, "unknown flux model");
+    if (flux_model < DMANN_FLUX_ANN_NOSOM || flux_model > DMANN_FLUX_ANN_ADIABATIC)
+        return fail(ctx, DMANN_ERR_INVALID, "unknown flux model");
     ctx->unit_factor = unit_factor;
     ctx->hires = hires_threshold;
     ctx->flux_model = flux_model;
@@ -359,6 +362,16 @@ dmann_status merge_tuning(dmann_ctx *ctx, const dmann_tuning &t, dmann_tuning &d
     return DMANN_OK;
 }
 }  // namespace
+
+dmann_status dmann_set_flux_params(dmann_ctx *ctx, double velocity_to_cgs, const double cpos[3]) {
+    if (!ctx || !cpos) return DMANN_ERR_INVALID;
+    if (!std::isfinite(velocity_to_cgs) || !std::isfinite(cpos[0]) || !std::isfinite(cpos[1]) ||
+        !std::isfinite(cpos[2]))
+        return fail(ctx, DMANN_ERR_INVALID, "non-finite flux parameter");
+    ctx->vel_to_cgs = velocity_to_cgs;
+    std::memcpy(ctx->fcpos, cpos, sizeof(double) * 3);
+    return DMANN_OK;
+}
 
 dmann_status dmann_set_tuning(dmann_ctx *ctx, const dmann_tuning *t) {
     if (!ctx || !t) return DMANN_ERR_INVALID;
@@ -424,7 +437,13 @@ Frame make_frame(const dmann_ctx *ctx, double *scale) {
     f.inv_scale = std::ldexp(1.0, -e2);  // FP32 deposits hold flux / 2^e2 (exact scaling)
     *scale = std::ldexp(1.0, e2);
     f.flux_model = ctx->flux_model;
+    f.vel_to_cgs = ctx->vel_to_cgs;
+    for (int i = 0; i < 3; i++) f.fcpos[i] = ctx->fcpos[i];
     return f;
+}
+
+bool law_needs_sigmav(int model) {
+    return model == DMANN_FLUX_ANN_SOMV || model == DMANN_FLUX_ANN_SOMV2 || model == DMANN_FLUX_ANN_PWAVE;
 }
 
 Accum make_accum(dmann_ctx *ctx) {
@@ -468,10 +487,18 @@ dmann_status dmann_map_begin(dmann_ctx *ctx, int nside, int precision) {
 
 dmann_status dmann_map_add(dmann_ctx *ctx, const float *x, const float *y, const float *z,
                            const float *m, const float *rho, const float *h, int64_t n) {
+    return dmann_map_add_v(ctx, x, y, z, m, rho, h, nullptr, n);
+}
+
+dmann_status dmann_map_add_v(dmann_ctx *ctx, const float *x, const float *y, const float *z,
+                             const float *m, const float *rho, const float *h,
+                             const float *sigmav, int64_t n) {
     if (!ctx) return DMANN_ERR_INVALID;
     if (!ctx->in_map) return fail(ctx, DMANN_ERR_STATE, "dmann_map_add outside begin/end");
     dmann_status st = check_particles(ctx, x, y, z, m, rho, h, n);
     if (st != DMANN_OK) return st;
+    if (n > 0 && !sigmav && law_needs_sigmav(ctx->flux_model))
+        return fail(ctx, DMANN_ERR_INVALID, "this flux law needs the velocity dispersion (dmann_map_add_v)");
     ctx->stats.n_in += n;
     if (n == 0) return DMANN_OK;
     CK(cudaSetDevice(ctx->device));
@@ -483,9 +510,10 @@ dmann_status dmann_map_add(dmann_ctx *ctx, const float *x, const float *y, const
         (st = ensure(ctx, ctx->queue, 4 * N)))
         return st;
     // inputs: device pointers are used in place, host arrays are copied
-    const float *src[6] = {x, y, z, m, rho, h};
-    const float *dev[6];
-    for (int k = 0; k < 6; k++) {
+    const float *src[7] = {x, y, z, m, rho, h, law_needs_sigmav(ctx->flux_model) ? sigmav : nullptr};
+    const float *dev[7] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    for (int k = 0; k < 7; k++) {
+        if (!src[k]) continue;
         if (is_device_ptr(src[k])) {
             dev[k] = src[k];
         } else {
@@ -503,7 +531,7 @@ dmann_status dmann_map_add(dmann_ctx *ctx, const float *x, const float *y, const
     CK(cudaMemsetAsync(ctx->hist.p, 0, 4 * (size_t)kKeys, s));
     CK(cudaMemsetAsync((long long *)ctx->ctr.p + kCtrChunkFirst, 0, 8 * (C_COUNT - kCtrChunkFirst), s));
     PrepArgs pa;
-    pa.p = {dev[0], dev[1], dev[2], dev[3], dev[4], dev[5], (int)N};
+    pa.p = {dev[0], dev[1], dev[2], dev[3], dev[4], dev[5], (int)N, dev[6]};
     pa.f = f;
     pa.g = ctx->g;
     pa.out = {(double *)ctx->theta.p, (double *)ctx->phi.p, (double *)ctx->ar.p,
@@ -573,12 +601,18 @@ dmann_status dmann_map_end(dmann_ctx *ctx, double *map_out, int accumulate) {
 dmann_status dmann_render(dmann_ctx *ctx, const float *x, const float *y, const float *z,
                           const float *m, const float *rho, const float *h, int64_t n, int nside,
                           int precision, double *map_out, int accumulate) {
+    return dmann_render_v(ctx, x, y, z, m, rho, h, nullptr, n, nside, precision, map_out, accumulate);
+}
+
+dmann_status dmann_render_v(dmann_ctx *ctx, const float *x, const float *y, const float *z,
+                            const float *m, const float *rho, const float *h, const float *sigmav,
+                            int64_t n, int nside, int precision, double *map_out, int accumulate) {
     if (!ctx) return DMANN_ERR_INVALID;
     if (!map_out) return fail(ctx, DMANN_ERR_INVALID, "map_out is null");
     dmann_status st = check_particles(ctx, x, y, z, m, rho, h, n);
     if (st != DMANN_OK) return st;
     if ((st = dmann_map_begin(ctx, nside, precision)) != DMANN_OK) return st;
-    if ((st = dmann_map_add(ctx, x, y, z, m, rho, h, n)) != DMANN_OK) {
+    if ((st = dmann_map_add_v(ctx, x, y, z, m, rho, h, sigmav, n)) != DMANN_OK) {
         ctx->in_map = false;
         return st;
     }
@@ -658,6 +692,8 @@ dmann_status dmann_render_batch(dmann_ctx *ctx, const float *x, const float *y, 
     if (precision != DMANN_PLAIN_F64 && precision != DMANN_COMP_F32)
         return fail(ctx, DMANN_ERR_INVALID, "unknown precision form");
     if (!ctx->have_units) return fail(ctx, DMANN_ERR_STATE, "units not set");
+    if (law_needs_sigmav(ctx->flux_model))
+        return fail(ctx, DMANN_ERR_INVALID, "the batch takes no velocity dispersion: render this flux law per observer");
     dmann_status st = check_particles(ctx, x, y, z, m, rho, h, n);
     if (st != DMANN_OK) return st;
     int maxns = 0;
@@ -751,6 +787,8 @@ dmann_status dmann_adjoint(dmann_ctx *ctx, const float *x, const float *y, const
     if (nside < 1 || nside > 8192) return fail(ctx, DMANN_ERR_INVALID, "nside must be in [1, 8192]");
     if (!ctx->have_frame) return fail(ctx, DMANN_ERR_STATE, "observer frame not set");
     if (!ctx->have_units) return fail(ctx, DMANN_ERR_STATE, "units not set");
+    if (ctx->flux_model != DMANN_FLUX_ANN_NOSOM)
+        return fail(ctx, DMANN_ERR_INVALID, "the adjoint supports the nosom flux law only");
     dmann_status st = check_particles(ctx, x, y, z, m, rho, h, n);
     if (st != DMANN_OK) return st;
     CK(cudaSetDevice(ctx->device));
@@ -887,6 +925,16 @@ dmann_status dmann_code_units(double h100, double Lbox_in_Mpc, double mass_to_Ms
     out[6] = u.velocity_to_cgs;
     out[7] = u.annihilation_flux_to_cgs;
     out[8] = nosom_unit_factor(u);
+    return DMANN_OK;
+}
+
+dmann_status dmann_flux_unit_factor(int flux_model, double h100, double Lbox_in_Mpc,
+                                    double mass_to_Msun, double *unit_factor) {
+    if (!unit_factor || flux_model < DMANN_FLUX_ANN_NOSOM || flux_model > DMANN_FLUX_ANN_ADIABATIC)
+        return DMANN_ERR_INVALID;
+    CodeUnits u;
+    setup_units(h100, Lbox_in_Mpc, mass_to_Msun, &u);
+    *unit_factor = flux_model == DMANN_FLUX_DECAY ? decay_unit_factor(u) : nosom_unit_factor(u);
     return DMANN_OK;
 }
 

@@ -28,7 +28,9 @@ struct Frame {
     double unit_factor;
     double hires_threshold;
     double inv_scale;     // power of two applied to fluxes deposited in FP32
-    int flux_model;
+    int flux_model;       // dmann_flux
+    double vel_to_cgs;    // code velocity unit (somv, somv2, pwave laws)
+    double fcpos[3];      // halo centre (adiabatic law)
 };
 
 // HEALPix constants of one Nside (src/datatypes.h:248-253 for dOmega).

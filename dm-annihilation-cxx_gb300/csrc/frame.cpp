@@ -186,6 +186,11 @@ double nosom_unit_factor(const CodeUnits &u) {
            u.annihilation_flux_to_cgs;
 }
 
+double decay_unit_factor(const CodeUnits &u) {
+    const double decay_flux_to_cgs = (u.mass_to_cgs / std::pow(u.length_to_cgs, 2));
+    return std::pow(c_in_cgs, 2) / (eV_in_cgs * 1.0e9) / (Mpc_in_cgs * 1.0e-3) * decay_flux_to_cgs;
+}
+
 double hires_threshold(const double *masses, int n) {
     float hires = FLT_MAX;
     for (int i = 0; i < n; i++)

@@ -27,6 +27,8 @@ struct CodeUnits {
 };
 void setup_units(double h100, double Lbox_in_Mpc, double mass_to_Msun, CodeUnits *u);
 double nosom_unit_factor(const CodeUnits &u);
+// The decay law's unit factor (src/flux/flux_decay.cpp:10-13).
+double decay_unit_factor(const CodeUnits &u);
 
 // genmap.cpp:52-58,82: the hires mass is held in a float; particles with
 // mass >= hires * 1.1 are skipped.  masses[0..n) are the particle_masses.

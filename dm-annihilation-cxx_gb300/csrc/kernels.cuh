@@ -29,6 +29,7 @@ constexpr int kCtrChunkFirst = C_ADD_DISC;
 struct Particles {
     const float *x, *y, *z, *m, *rho, *h;
     int n;
+    const float *sigmav;   // velocity dispersion; only the laws that use it read it
 };
 
 // Per-particle geometry written by the prep kernel (FP64).

@@ -47,6 +47,51 @@ __device__ inline void count_warp(long long *ctr, bool pred) {
     if ((threadIdx.x & 31) == 0 && b) atomicAdd((unsigned long long *)ctr, (unsigned long long)__popc(b));
 }
 
+constexpr double kCinCgs = 2.99792458e10;   // src/datatypes.cpp:5-10
+
+// getflux of the context's flux law (the reference's link-time plugins in
+// src/flux), each in its plugin's operation order.
+__device__ inline double particle_flux(const PrepArgs &a, int i, float mass, float dens, double d) {
+    const double uf = a.f.unit_factor;
+    switch (a.f.flux_model) {
+    case 1: {  // flux_ann_somv.cpp:16-43: <sigma v> ~ 1/v, saturated at 1 km/s, / 1e4
+        double v = (double)a.p.sigmav[i] * a.f.vel_to_cgs;
+        v /= 1.0e5;
+        if (v < 1) v = 1;
+        const double somer_v = kCinCgs / v / 1.0e4;
+        return uf * somer_v * (double)dens * (double)mass / (4.0 * kPi * d * d);
+    }
+    case 2: {  // flux_ann_somv2.cpp:16-44: ~ 1/v^2, saturated at 5 km/s, / 1e8
+        double v = (double)a.p.sigmav[i] * a.f.vel_to_cgs;
+        v /= 1.0e5;
+        if (v < 5) v = 5;
+        double somer_v = kCinCgs / v;
+        somer_v *= (somer_v / 1.0e8);
+        return uf * somer_v * (double)dens * (double)mass / (4.0 * kPi * d * d);
+    }
+    case 3: {  // flux_ann_pwave.cpp:13-31: ~ v^2
+        double somer_v = ((double)a.p.sigmav[i] * a.f.vel_to_cgs) / kCinCgs;
+        somer_v = somer_v * somer_v;
+        return uf * somer_v * (double)dens * (double)mass / (4.0 * kPi * d * d);
+    }
+    case 4:    // flux_decay.cpp:9-16 (unit_factor is the decay law's own)
+        return uf * (double)mass / (4.0 * kPi * d * d);
+    case 5: {  // flux_ann_adiabatic.cpp:10-33: adiabatic-contraction boost of the host
+        const double dx = (double)a.p.x[i] - a.f.fcpos[0];
+        const double dy = (double)a.p.y[i] - a.f.fcpos[1];
+        const double dz = (double)a.p.z[i] - a.f.fcpos[2];
+        const double r = sqrt(dx * dx + dy * dy + dz * dz) * 40000.0;
+        const double factor = (14.6534 * pow(1 + 0.0355872 * r, 1.76)) /
+                               (pow(1 + 0.10888 * pow(r, 0.76), 3.34211) * pow(r, 0.13));
+        double fluxes = uf * (double)dens * (double)mass / (4.0 * kPi * d * d);
+        fluxes *= (factor * factor);
+        return fluxes;
+    }
+    default:   // flux_ann_nosom.cpp:18
+        return uf * (double)dens * (double)mass / (4.0 * kPi * d * d);
+    }
+}
+
 __global__ void __launch_bounds__(256) k_prep(PrepArgs a) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const bool in = i < a.p.n;
@@ -63,8 +108,7 @@ __global__ void __launch_bounds__(256) k_prep(PrepArgs a) {
             const double dy = (double)py - a.f.opos[1];
             const double dz = (double)pz - a.f.opos[2];
             const double d = sqrt(dx * dx + dy * dy + dz * dz);  // genmap.cpp:87-89
-            // flux_ann_nosom.cpp:18
-            flux = a.f.unit_factor * (double)dens * (double)mass / (4.0 * kPi * d * d);
+            flux = particle_flux(a, i, mass, dens, d);
             // anglefuncs.cpp:15-52: v' = rot^T v, cos(theta) = v'_z/d, phi shifted by pi
             double t[3];
             const double v[3] = {dx, dy, dz};

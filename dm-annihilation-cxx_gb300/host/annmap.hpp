@@ -91,6 +91,8 @@ public:
 
     // Mass at or above which a particle is skipped (genmap.cpp:52-58).
     double hiresThreshold() const;
+    // The unit factor of a flux law (dmann_flux_unit_factor).
+    double fluxUnitFactor(int flux_model) const;
     // Moves the observer (and optionally the alignment vector) and redoes the
     // rotation; the reference keeps these private.
     void setObserver(const double opos[3], const double *align = nullptr);
@@ -146,8 +148,10 @@ private:
 
 class MapGenerator {
 public:
+    // flux_model: a dmann_flux law (the reference links one getflux plugin
+    // per build; here it is chosen per generator).
     MapGenerator(Parameters *par, DataReader *reader, int precision = DMANN_COMP_F32,
-                 int device = 0);
+                 int device = 0, int flux_model = DMANN_FLUX_ANN_NOSOM);
     ~MapGenerator();
     MapGenerator(const MapGenerator &) = delete;
     MapGenerator &operator=(const MapGenerator &) = delete;
@@ -163,7 +167,7 @@ public:
 private:
     Parameters *par_;
     DataReader *reader_;
-    int precision_, device_;
+    int precision_, device_, flux_model_;
     bool isFinished_ = false;
     MAPTYPE *map_ = nullptr;
     double total_flux_ = 0;

@@ -76,10 +76,11 @@ int64_t annmap_read_native(const char *path, const char *maskfile, int test, int
 
 // The reference's main flow (src/main.cpp:35-66) on the GPU: Parameters,
 // DataReader (test limit and buffer from the info file), MapGenerator::start,
-// and saveToFits to the info file's outputmap when it names one.  map_out
+// and saveToFits to the info file's outputmap when it names one, with the
+// flux law flux_model (dmann_flux).  map_out
 // receives the 12 nside^2 map (npix must match); total_flux the "Total Conts".
-int annmap_genmap(const char *info_file, int precision, int device, double *map_out, int64_t npix,
-                  double *total_flux, char *err, int errlen) {
+int annmap_genmap(const char *info_file, int precision, int device, int flux_model,
+                  double *map_out, int64_t npix, double *total_flux, char *err, int errlen) {
     try {
         annmap::Parameters par(info_file);
         if (!par.isNative) return fail(err, errlen, "only native particle files are supported");
@@ -88,7 +89,7 @@ int annmap_genmap(const char *info_file, int precision, int device, double *map_
         reader.setTest(par.testNum);
         reader.setBuf((unsigned)par.memParts);
         reader.open();
-        annmap::MapGenerator gen(&par, &reader, precision, device);
+        annmap::MapGenerator gen(&par, &reader, precision, device, flux_model);
         gen.start();
         reader.close();
         std::memcpy(map_out, gen.getMap(), sizeof(double) * (size_t)npix);

@@ -45,14 +45,14 @@ void cuda_check(cudaError_t e, const char *what) {
 // The pinned and device buffers of the two pipeline slots.
 struct Slots {
     size_t cap = 0;
-    float *host[2] = {nullptr, nullptr};   // 6 * cap floats each (pinned)
+    float *host[2] = {nullptr, nullptr};   // 7 * cap floats each (pinned): x y z m rho h sigmav
     float *dev[2] = {nullptr, nullptr};
     cudaEvent_t done[2] = {nullptr, nullptr};
     explicit Slots(size_t capacity) : cap(capacity) {
         for (int k = 0; k < 2; k++) {
-            cuda_check(cudaHostAlloc((void **)&host[k], 6 * cap * sizeof(float), cudaHostAllocDefault),
+            cuda_check(cudaHostAlloc((void **)&host[k], 7 * cap * sizeof(float), cudaHostAllocDefault),
                        "pinned chunk buffer");
-            cuda_check(cudaMalloc((void **)&dev[k], 6 * cap * sizeof(float)), "device chunk buffer");
+            cuda_check(cudaMalloc((void **)&dev[k], 7 * cap * sizeof(float)), "device chunk buffer");
             cuda_check(cudaEventCreateWithFlags(&done[k], cudaEventDisableTiming), "event");
         }
     }
@@ -67,15 +67,18 @@ struct Slots {
 
 }  // namespace
 
-MapGenerator::MapGenerator(Parameters *par, DataReader *reader, int precision, int device)
-    : par_(par), reader_(reader), precision_(precision), device_(device) {}
+MapGenerator::MapGenerator(Parameters *par, DataReader *reader, int precision, int device,
+                           int flux_model)
+    : par_(par), reader_(reader), precision_(precision), device_(device), flux_model_(flux_model) {}
 
 MapGenerator::~MapGenerator() { std::free(map_); }
 
 void MapGenerator::start() {
     Ctx ctx(device_);
     ctx.check(dmann_set_frame(ctx.c, &par_->rotmatrix[0][0], par_->params.opos));
-    ctx.check(dmann_set_units(ctx.c, par_->unit_factor, par_->hiresThreshold(), DMANN_FLUX_ANN_NOSOM));
+    ctx.check(dmann_set_units(ctx.c, par_->fluxUnitFactor(flux_model_), par_->hiresThreshold(),
+                              flux_model_));
+    ctx.check(dmann_set_flux_params(ctx.c, par_->codeunits.velocity_to_cgs, par_->params.cpos));
     cuda_check(cudaSetDevice(device_), "cudaSetDevice");
     cudaStream_t s = nullptr;
     cuda_check(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking), "stream");
@@ -103,7 +106,7 @@ void MapGenerator::start() {
             float *h = slots.host[slot], *d = slots.dev[slot];
             const size_t cap = slots.cap;
             float *hx = h, *hy = h + cap, *hz = h + 2 * cap, *hm = h + 3 * cap, *hr = h + 4 * cap,
-                  *hh = h + 5 * cap;
+                  *hh = h + 5 * cap, *hv = h + 6 * cap;
             for (size_t i = 0; i < n; i++) {   // records -> SoA
                 hx[i] = p[i].posx;
                 hy[i] = p[i].posy;
@@ -111,13 +114,14 @@ void MapGenerator::start() {
                 hm[i] = p[i].mass;
                 hr[i] = p[i].dens;
                 hh[i] = p[i].hsmooth;
+                hv[i] = p[i].sigmav;
             }
-            for (int f = 0; f < 6; f++)
+            for (int f = 0; f < 7; f++)
                 cuda_check(cudaMemcpyAsync(d + f * cap, h + f * cap, n * sizeof(float),
                                            cudaMemcpyHostToDevice, s),
                            "chunk upload");
-            ctx.check(dmann_map_add(ctx.c, d, d + cap, d + 2 * cap, d + 3 * cap, d + 4 * cap,
-                                    d + 5 * cap, (int64_t)n));
+            ctx.check(dmann_map_add_v(ctx.c, d, d + cap, d + 2 * cap, d + 3 * cap, d + 4 * cap,
+                                      d + 5 * cap, d + 6 * cap, (int64_t)n));
             cuda_check(cudaEventRecord(slots.done[slot], s), "chunk event");
             reader_->loadBuffer();   // genmap.cpp:155, overlapping the GPU work
             k++;

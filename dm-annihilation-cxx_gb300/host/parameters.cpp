@@ -166,6 +166,14 @@ void Parameters::setObserver(const double opos[3], const double *align) {
     params.ophi = ang[1];
 }
 
+double Parameters::fluxUnitFactor(int flux_model) const {
+    if (flux_model == DMANN_FLUX_ANN_NOSOM) return unit_factor;
+    double u = 0;
+    if (dmann_flux_unit_factor(flux_model, info.h100, info.Lbox_in_Mpc, info.mass_to_Msun, &u) != DMANN_OK)
+        throw std::runtime_error("unknown flux law");
+    return u;
+}
+
 double Parameters::hiresThreshold() const {
     return dmann_hires_threshold(params.particle_masses, MAX_NUM_MASS_RES);
 }

@@ -96,10 +96,19 @@ class Renderer:
         self._check(self.L.dmann_set_units(self.ctx, float(unit_factor), float(hires_threshold),
                                            int(flux_model)))
 
-    def set_params(self, par):
-        """Frame and units from a Parameters object."""
+    def set_flux_params(self, velocity_to_cgs: float, cpos=(0.0, 0.0, 0.0)):
+        """Constants of the flux laws: code velocity unit, halo centre."""
+        self._check(self.L.dmann_set_flux_params(self.ctx, float(velocity_to_cgs),
+                                                 (C.c_double * 3)(*[float(v) for v in cpos])))
+
+    def set_params(self, par, flux_model: int = 0):
+        """Frame, units and flux law from a Parameters object (flux_model is
+        a dmann_flux value or a law name such as "ann_somv")."""
+        if isinstance(flux_model, str):
+            flux_model = _lib.FLUX_LAWS[flux_model]
         self.set_frame(par.rotmatrix, par.params.opos)
-        self.set_units(par.unit_factor, par.hires_threshold)
+        self.set_units(par.flux_unit_factor(flux_model), par.hires_threshold, flux_model)
+        self.set_flux_params(par.codeunits.velocity_to_cgs, par.params.cpos)
 
     def set_tuning(self, nside: int | None = None, **kw):
         """Default tuning, or the entry for maps of ``nside``
@@ -130,13 +139,17 @@ class Renderer:
         self._check(self.L.dmann_map_begin(self.ctx, int(nside), int(precision)))
 
     def add(self, parts: dict):
+        """Deposits one chunk: float32 arrays x, y, z, m, rho, h and, for the
+        flux laws that use it, the velocity dispersion "sigmav"."""
         arrays = [parts[k] for k in FIELDS]
         n = len(arrays[0])
-        if any(len(a) != n for a in arrays):
+        sv = parts.get("sigmav")
+        if any(len(a) != n for a in arrays) or (sv is not None and len(sv) != n):
             raise ValueError("particle arrays differ in length")
-        self._use_torch_stream(arrays)
+        self._use_torch_stream(arrays + ([sv] if sv is not None else []))
         ptrs = [self._ptr(a, np.float32) for a in arrays]
-        self._check(self.L.dmann_map_add(self.ctx, *ptrs, int(n)))
+        svp = self._ptr(sv, np.float32) if sv is not None else None
+        self._check(self.L.dmann_map_add_v(self.ctx, *ptrs, svp, int(n)))
 
     def end(self, out=None, accumulate: bool = False):
         npix = 12 * self._nside * self._nside
@@ -232,11 +245,12 @@ class Renderer:
 class MapGenerator:
     """The reference's MapGenerator (src/mapgenerator.h:8-26) on the GPU."""
 
-    def __init__(self, par, reader, precision: int = COMP_F32, device: int = 0):
+    def __init__(self, par, reader, precision: int = COMP_F32, device: int = 0, flux_model=0):
         self.par_ = par
         self.reader_ = reader
         self.precision = precision
         self.device = device
+        self.flux_model = flux_model   # the reference's link-time getflux plugin, chosen here
         self.map_ = None
         self.isFinished_ = False
         self.total_flux = None
@@ -244,7 +258,7 @@ class MapGenerator:
     def start(self):
         r = Renderer(self.device)
         try:
-            r.set_params(self.par_)
+            r.set_params(self.par_, self.flux_model)
             r.begin(self.par_.map.Nside, self.precision)
             while self.reader_.hasNext():
                 r.add(self.reader_.next_chunk())

@@ -240,6 +240,18 @@ class Parameters:
         self.map.setNside(nside)
 
     # ------------------------------------------------------------------ derived
+    def flux_unit_factor(self, flux_model: int = 0) -> float:
+        """The unit factor of a flux law (dmann_flux_unit_factor): the
+        annihilation laws share unit_factor, the decay law has its own."""
+        if flux_model == 0:
+            return self.unit_factor
+        L = _lib.load()
+        out = (C.c_double * 1)()
+        if L.dmann_flux_unit_factor(int(flux_model), self.info["h100"], self.info["Lbox_in_Mpc"],
+                                    self.info["mass_to_Msun"], out) != 0:
+            raise ValueError("unknown flux law")
+        return out[0]
+
     @property
     def hires_threshold(self) -> float:
         L = _lib.load()

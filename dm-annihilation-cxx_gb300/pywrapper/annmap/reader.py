@@ -8,8 +8,9 @@ zero byte marks the particle as masked by setting dens = -1
 (src/datareader.cpp:263-271).  ``setTest(n)`` limits the stream to the first
 n particles (src/datareader.cpp:202-206); ``setBuf(n)`` sets the chunk size.
 
-The reader yields float32 SoA chunks (x, y, z, m, rho, h) -- the layout the
-GPU kernels read -- instead of the 48-byte AoS records.
+The reader yields float32 SoA chunks (x, y, z, m, rho, h, and the velocity
+dispersion sigmav some flux laws read) -- the layout the GPU kernels read --
+instead of the 48-byte AoS records.
 """
 from __future__ import annotations
 
@@ -79,7 +80,8 @@ class DataReader:
         self._cursor = i1
         return {"x": np.ascontiguousarray(rec["posx"]), "y": np.ascontiguousarray(rec["posy"]),
                 "z": np.ascontiguousarray(rec["posz"]), "m": np.ascontiguousarray(rec["mass"]),
-                "rho": rho, "h": np.ascontiguousarray(rec["hsmooth"])}
+                "rho": rho, "h": np.ascontiguousarray(rec["hsmooth"]),
+                "sigmav": np.ascontiguousarray(rec["sigmav"])}
 
     def close(self):
         self._mm = None

@@ -72,9 +72,19 @@ typedef enum {
     DMANN_COMP_F32 = 1
 } dmann_precision;
 
-/* Flux laws (the reference's link-time getflux plugins, src/flux/). */
+/* Flux laws: the reference's link-time getflux plugins (the files of src/flux,
+ * src/flux.h:6), selected per context at run time.  unit_factor is the
+ * law's factor (dmann_flux_unit_factor); v = sigmav * velocity_to_cgs / 1e5 is
+ * the velocity dispersion in km/s, c the speed of light in cm/s.  Each law
+ * keeps its plugin's operation order. */
 typedef enum {
-    DMANN_FLUX_ANN_NOSOM = 0   /* unit_factor * rho * m / (4 pi d^2) */
+    DMANN_FLUX_ANN_NOSOM = 0,     /* unit_factor rho m / (4 pi d^2)   flux_ann_nosom.cpp */
+    DMANN_FLUX_ANN_SOMV = 1,      /* x c / max(v, 1) / 1e4           flux_ann_somv.cpp */
+    DMANN_FLUX_ANN_SOMV2 = 2,     /* x (c / max(v, 5))^2 / 1e8       flux_ann_somv2.cpp */
+    DMANN_FLUX_ANN_PWAVE = 3,     /* x (sigmav velocity_to_cgs / c)^2 flux_ann_pwave.cpp */
+    DMANN_FLUX_DECAY = 4,         /* unit_factor m / (4 pi d^2)      flux_decay.cpp */
+    DMANN_FLUX_ANN_ADIABATIC = 5  /* nosom x f(r)^2, r = |pos - cpos| * 40000
+                                     (kpc/h in the reference's units) flux_ann_adiabatic.cpp */
 } dmann_flux;
 
 /* Counters of the last dmann_render call on a context. */
@@ -130,11 +140,16 @@ dmann_status dmann_set_observer(dmann_ctx *ctx, const double opos[3],
  * calc_angles (v' = rot^T (pos - opos)). */
 dmann_status dmann_set_frame(dmann_ctx *ctx, const double rot[9],
                              const double opos[3]);
-/* unit_factor multiplies rho*m/(4 pi d^2); hires_threshold is the mass at or
- * above which a particle is skipped ((double)(float)min_mass * 1.1 in the
- * reference; pass INFINITY to keep every particle). */
+/* unit_factor multiplies the flux law (dmann_flux); hires_threshold is the
+ * mass at or above which a particle is skipped ((double)(float)min_mass * 1.1
+ * in the reference; pass INFINITY to keep every particle). */
 dmann_status dmann_set_units(dmann_ctx *ctx, double unit_factor,
                              double hires_threshold, int flux_model);
+/* The constants some flux laws read besides unit_factor: the code velocity
+ * unit (somv, somv2, pwave; Parameters' codeunits.velocity_to_cgs) and the
+ * halo centre (adiabatic; params.cpos).  Default 0 and the origin. */
+dmann_status dmann_set_flux_params(dmann_ctx *ctx, double velocity_to_cgs,
+                                   const double cpos[3]);
 /* The context's default tuning (DMANN_ERR_INVALID for a block shape other
  * than 128/256/512 or negative values). */
 dmann_status dmann_set_tuning(dmann_ctx *ctx, const dmann_tuning *t);
@@ -160,6 +175,16 @@ dmann_status dmann_render(dmann_ctx *ctx, const float *x, const float *y,
                           const float *h, int64_t n, int nside, int precision,
                           double *map_out, int accumulate);
 
+/* dmann_render with each particle's velocity dispersion sigmav (code units,
+ * the native record's field, src/datatypes.h:46-59), which the somv, somv2
+ * and pwave laws need (the plain calls fail with DMANN_ERR_INVALID for those
+ * laws); other laws ignore it and accept NULL. */
+dmann_status dmann_render_v(dmann_ctx *ctx, const float *x, const float *y,
+                            const float *z, const float *m, const float *rho,
+                            const float *h, const float *sigmav, int64_t n,
+                            int nside, int precision, double *map_out,
+                            int accumulate);
+
 /* Streaming form of dmann_render, the shape of MapGenerator::start's loop
  * over DataReader chunks (src/genmap.cpp:67-156): begin zeroes the
  * context's device accumulation planes for one map, every add deposits one
@@ -172,6 +197,10 @@ dmann_status dmann_map_add(dmann_ctx *ctx, const float *x, const float *y,
                            const float *z, const float *m, const float *rho,
                            const float *h, int64_t n);
 dmann_status dmann_map_end(dmann_ctx *ctx, double *map_out, int accumulate);
+/* dmann_map_add with the velocity dispersion (as dmann_render_v). */
+dmann_status dmann_map_add_v(dmann_ctx *ctx, const float *x, const float *y,
+                             const float *z, const float *m, const float *rho,
+                             const float *h, const float *sigmav, int64_t n);
 
 /* Renders the same particles for n_obs observers in one call (no reference
  * counterpart: the reference renders one observer per run).  Observer k has
@@ -282,6 +311,11 @@ dmann_status dmann_observer_rotation_jacobian(const double opos[3],
  * = -1 derives the mass unit from rho_crit * L^3, as the reference does. */
 dmann_status dmann_code_units(double h100, double Lbox_in_Mpc,
                               double mass_to_Msun, double out[9]);
+/* The unit factor of a flux law from the code units of Parameters::setupUnits:
+ * the annihilation laws share flux_ann_nosom.cpp:13-16's factor, the decay
+ * law has its own (flux_decay.cpp:10-13). */
+dmann_status dmann_flux_unit_factor(int flux_model, double h100, double Lbox_in_Mpc,
+                                    double mass_to_Msun, double *unit_factor);
 /* src/genmap.cpp:52-58: (double)(float)min(masses > 0) * 1.1, the mass at
  * or above which a particle is skipped (FLT_MAX * 1.1 if none positive). */
 double dmann_hires_threshold(const double *masses, int n);

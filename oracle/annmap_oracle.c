@@ -53,6 +53,10 @@ void orc_params_setup(orc_params *p) {
     p->unit_factor = pow(pow(c_in_cgs, 2) / (eV_in_cgs * 1.0e9), 2) /
                      (Mpc_in_cgs * 1.0e-3) * p->annihilation_flux_to_cgs;
 
+    /* src/flux/flux_decay.cpp:10-13 */
+    p->decay_unit_factor = pow(c_in_cgs, 2) / (eV_in_cgs * 1.0e9) / (Mpc_in_cgs * 1.0e-3) *
+                           (p->mass_to_cgs / pow(p->length_to_cgs, 2));
+
     /* src/parameters.cpp:111-152 setupParams: observer angles about the centre */
     const double *opos = p->obs_pos, *cpos = p->centerpos;
     double radius = sqrt(pow(opos[0] - cpos[0], 2.0) + pow(opos[1] - cpos[1], 2.0) +
@@ -150,19 +154,63 @@ typedef struct {
     int kept;
 } geom_t;
 
+/* getflux of the flux law p->flux_model for one particle at distance d, each
+ * in the operation order of its plugin (sigmav only read by the laws that
+ * use it). */
+static double orc_flux(const orc_params *p, double mass, double dens, double sigmav,
+                       double px, double py, double pz, double d) {
+    const double uf = p->unit_factor;
+    switch (p->flux_model) {
+    case ORC_FLUX_SOMV: { /* src/flux/flux_ann_somv.cpp:16-43: SAT_V 1 km/s, FACTOR 1e4 */
+        double v = sigmav * p->velocity_to_cgs;
+        v /= 1.0e5;
+        if (v < 1) v = 1;
+        double somer_v = c_in_cgs / v / 1.0e4;
+        return uf * somer_v * dens * mass / (4.0 * PI * d * d);
+    }
+    case ORC_FLUX_SOMV2: { /* src/flux/flux_ann_somv2.cpp:16-44: SAT_V 5 km/s, FACTOR 1e8 */
+        double v = sigmav * p->velocity_to_cgs;
+        v /= 1.0e5;
+        if (v < 5) v = 5;
+        double somer_v = c_in_cgs / v;
+        somer_v *= (somer_v / 1.0e8);
+        return uf * somer_v * dens * mass / (4.0 * PI * d * d);
+    }
+    case ORC_FLUX_PWAVE: { /* src/flux/flux_ann_pwave.cpp:13-31 */
+        double somer_v = (sigmav * p->velocity_to_cgs) / c_in_cgs;
+        somer_v = somer_v * somer_v;
+        return uf * somer_v * dens * mass / (4.0 * PI * d * d);
+    }
+    case ORC_FLUX_DECAY: /* src/flux/flux_decay.cpp:9-16 */
+        return p->decay_unit_factor * mass / (4.0 * PI * d * d);
+    case ORC_FLUX_ADIABATIC: { /* src/flux/flux_ann_adiabatic.cpp:10-33 */
+        double dx = px - p->centerpos[0];
+        double dy = py - p->centerpos[1];
+        double dz = pz - p->centerpos[2];
+        double r = sqrt(dx * dx + dy * dy + dz * dz) * 40000.0;
+        double factor = (14.6534 * pow(1 + 0.0355872 * r, 1.76)) /
+                        (pow(1 + 0.10888 * pow(r, 0.76), 3.34211) * pow(r, 0.13));
+        double fluxes = uf * dens * mass / (4.0 * PI * d * d);
+        fluxes *= (factor * factor);
+        return fluxes;
+    }
+    default: /* src/flux/flux_ann_nosom.cpp:12-23 */
+        return uf * dens * mass / (4.0 * PI * d * d);
+    }
+}
+
 /* genmap.cpp:82-106 for one particle.  The inputs are the float values
  * promoted to double (the finite-difference checks pass unrounded doubles). */
-static void particle_geom_d(const orc_params *p, const orc_hpx *hb, double mass,
-                            double dens, double hsmooth, double px, double py,
-                            double pz, geom_t *g) {
+static void particle_geom_dv(const orc_params *p, const orc_hpx *hb, double mass,
+                             double dens, double hsmooth, double px, double py,
+                             double pz, double sigmav, geom_t *g) {
     g->kept = 0;
     if (mass >= p->hires_threshold || dens < 0) return;
     g->kept = 1;
     double ox = p->obs_pos[0], oy = p->obs_pos[1], oz = p->obs_pos[2];
     double dx = px - ox, dy = py - oy, dz = pz - oz;
     g->d = sqrt(dx * dx + dy * dy + dz * dz);
-    /* flux_ann_nosom.cpp:18: unit_factor * dens * mass / (4 PI d d) */
-    g->flux = p->unit_factor * dens * mass / (4.0 * PI * g->d * g->d);
+    g->flux = orc_flux(p, mass, dens, sigmav, px, py, pz, g->d);
     calc_angles(dx, dy, dz, g->d, p, &g->costheta, &g->phi);
     double ct = g->costheta;
     if (ct > 1.0) ct = 1.0; /* acos argument guard */
@@ -170,6 +218,12 @@ static void particle_geom_d(const orc_params *p, const orc_hpx *hb, double mass,
     g->theta = acos(ct);
     g->ar = hsmooth / g->d;
     g->pix = orc_hpx_ang2pix(hb, g->theta, g->phi);
+}
+
+static void particle_geom_d(const orc_params *p, const orc_hpx *hb, double mass,
+                            double dens, double hsmooth, double px, double py,
+                            double pz, geom_t *g) {
+    particle_geom_dv(p, hb, mass, dens, hsmooth, px, py, pz, 0.0, g);
 }
 
 static void particle_geom(const orc_params *p, const orc_hpx *hb, float mass,
@@ -198,7 +252,7 @@ void orc_particle_geom(const orc_params *p, float mass, float dens,
 
 typedef struct {
     const orc_params *p;
-    const float *m, *rho, *h, *x, *y, *z;
+    const float *m, *rho, *h, *x, *y, *z, *sv;
     int64_t i0, i1;
     double *map;
     orc_stats st;
@@ -222,8 +276,9 @@ static void *render_range(void *arg) {
     memset(&J->st, 0, sizeof J->st);
     for (int64_t i = J->i0; i < J->i1; i++) {
         geom_t g;
-        particle_geom(p, &hb, J->m[i], J->rho[i], J->h[i], J->x[i], J->y[i],
-                      J->z[i], &g);
+        particle_geom_dv(p, &hb, (double)J->m[i], (double)J->rho[i], (double)J->h[i],
+                         (double)J->x[i], (double)J->y[i], (double)J->z[i],
+                         J->sv ? (double)J->sv[i] : 0.0, &g);
         if (!g.kept) {
             J->st.skipped++;
             continue;
@@ -278,6 +333,13 @@ int orc_render(const orc_params *p, const float *mass, const float *dens,
                const float *hsmooth, const float *x, const float *y,
                const float *z, int64_t n, double *map, orc_stats *stats,
                int nthreads) {
+    return orc_render_v(p, mass, dens, hsmooth, x, y, z, NULL, n, map, stats, nthreads);
+}
+
+int orc_render_v(const orc_params *p, const float *mass, const float *dens,
+                 const float *hsmooth, const float *x, const float *y,
+                 const float *z, const float *sigmav, int64_t n, double *map,
+                 orc_stats *stats, int nthreads) {
     if (nthreads < 1) nthreads = 1;
     if (n < (int64_t)nthreads * 4) nthreads = 1;
     job_t *jobs = (job_t *)calloc((size_t)nthreads, sizeof(job_t));
@@ -292,7 +354,7 @@ int orc_render(const orc_params *p, const float *mass, const float *dens,
         job_t *J = &jobs[t];
         J->p = p;
         J->m = mass; J->rho = dens; J->h = hsmooth;
-        J->x = x; J->y = y; J->z = z;
+        J->x = x; J->y = y; J->z = z; J->sv = sigmav;
         J->i0 = n * t / nthreads;
         J->i1 = n * (t + 1) / nthreads;
         if (nthreads == 1) {

@@ -79,7 +79,15 @@ typedef struct {
     double hires_threshold;   /* (double)(float)min(particle_masses>0) * 1.1 */
     int64_t npix;
     double dOmega, theta0;    /* theta0 = acos(1 - dOmega/(2*3.141592)) */
+    /* flux law (set before orc_params_setup; 0 = nosom): the reference's
+     * link-time getflux plugins in the src/flux directory, see orc_flux */
+    int flux_model;
+    double decay_unit_factor; /* flux_decay.cpp:10-13 (derived) */
 } orc_params;
+
+/* Flux laws, in the numbering of the C ABI's dmann_flux. */
+enum { ORC_FLUX_NOSOM = 0, ORC_FLUX_SOMV = 1, ORC_FLUX_SOMV2 = 2, ORC_FLUX_PWAVE = 3,
+       ORC_FLUX_DECAY = 4, ORC_FLUX_ADIABATIC = 5 };
 
 /* Fills every derived field from the inputs (setupUnits, setupParams,
  * setupRotation, setNside and the per-map constants of genmap.cpp). */
@@ -100,6 +108,13 @@ int orc_render(const orc_params *p, const float *mass, const float *dens,
                const float *hsmooth, const float *x, const float *y,
                const float *z, int64_t n, double *map, orc_stats *stats,
                int nthreads);
+
+/* orc_render with the particles' velocity dispersion sigmav (float32, code
+ * units; needed by the somv, somv2 and pwave laws, may be NULL otherwise). */
+int orc_render_v(const orc_params *p, const float *mass, const float *dens,
+                 const float *hsmooth, const float *x, const float *y,
+                 const float *z, const float *sigmav, int64_t n, double *map,
+                 orc_stats *stats, int nthreads);
 
 /* genmap.cpp:161-169: returns totalC = sum(map) and divides map by dOmega. */
 double orc_finalize(const orc_params *p, double *map);

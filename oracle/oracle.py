@@ -41,6 +41,7 @@ class OrcParams(C.Structure):
         ("rotmatrix", (C.c_double * 3) * 3),
         ("unit_factor", C.c_double), ("hires_threshold", C.c_double),
         ("npix", C.c_int64), ("dOmega", C.c_double), ("theta0", C.c_double),
+        ("flux_model", C.c_int), ("decay_unit_factor", C.c_double),
     ]
 
 
@@ -87,6 +88,9 @@ def lib():
             L.orc_render.argtypes = [P(OrcParams), f32, f32, f32, f32, f32, f32, C.c_int64,
                                      P(C.c_double), P(OrcStats), C.c_int]
             L.orc_render.restype = C.c_int
+            L.orc_render_v.argtypes = [P(OrcParams), f32, f32, f32, f32, f32, f32, f32, C.c_int64,
+                                       P(C.c_double), P(OrcStats), C.c_int]
+            L.orc_render_v.restype = C.c_int
             L.orc_finalize.argtypes = [P(OrcParams), P(C.c_double)]
             L.orc_finalize.restype = C.c_double
             L.orc_particle_geom.argtypes = [P(OrcParams), C.c_float, C.c_float, C.c_float,
@@ -150,8 +154,9 @@ class Healpix:
 # ---------------------------------------------------------------- params
 def make_params(*, nside, obs_pos, centerpos, align_vec, h100=0.73, Omega_M=0.238,
                 Lbox_in_Mpc=0.001, mass_to_Msun=1.0, particle_masses=(0.0,),
-                redshift=0.0) -> OrcParams:
+                redshift=0.0, flux_model=0) -> OrcParams:
     p = OrcParams()
+    p.flux_model = int(flux_model)
     p.h100, p.Omega_M, p.Lbox_in_Mpc, p.mass_to_Msun, p.redshift = (
         h100, Omega_M, Lbox_in_Mpc, mass_to_Msun, redshift)
     for i in range(3):
@@ -183,10 +188,14 @@ def render(p: OrcParams, parts: dict, nthreads: int = 1, finalize: bool = True):
         keep.append(a)
         ptrs.append(ptr)
     n = len(keep[0])
+    sv = None
+    if parts.get("sigmav") is not None:
+        sva, sv = _f32(parts["sigmav"])
+        keep.append(sva)
     mp = np.zeros(int(p.npix), dtype=np.float64)
     st = OrcStats()
-    rc = lib().orc_render(C.byref(p), *ptrs, n, mp.ctypes.data_as(C.POINTER(C.c_double)),
-                          C.byref(st), int(nthreads))
+    rc = lib().orc_render_v(C.byref(p), *ptrs, sv, n, mp.ctypes.data_as(C.POINTER(C.c_double)),
+                            C.byref(st), int(nthreads))
     if rc != 0:
         raise RuntimeError("oracle render failed")
     total = None

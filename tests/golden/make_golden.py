@@ -35,8 +35,10 @@ def build_ref():
     subprocess.run(["make", "-s", "-C", os.path.join(REPO, "oracle", "ref_shim")], check=True)
 
 
-def write_native(path, P, extra_mass=None):
+def write_native(path, P, extra_mass=None, sigmav=None):
     rec = np.zeros((len(P), 12), np.float32)
+    if sigmav is not None:
+        rec[:, 9] = sigmav
     rec[:, 0] = P.m if extra_mass is None else extra_mass
     rec[:, 1] = P.rho
     rec[:, 2] = P.h
@@ -59,9 +61,9 @@ def parse_params(text):
 
 def run_case(name, P, *, nside, info_extra="", mass=None, mask=None, particle_masses=None,
              obs=None, centre=(0.0, 0.0, 0.0), align=(0.0, 0.0, 1.0), units="kpc",
-             mem_buffer=1000, test=None):
+             mem_buffer=1000, test=None, law="ann_nosom", sigmav=None):
     d = tempfile.mkdtemp(prefix="golden_")
-    rec = write_native(os.path.join(d, "parts.bin"), P, extra_mass=mass)
+    rec = write_native(os.path.join(d, "parts.bin"), P, extra_mass=mass, sigmav=sigmav)
     obs = P.obs_pos if obs is None else obs
     pm = particle_masses if particle_masses is not None else [P.particle_mass]
     lines = ["# golden case " + name, "Omega_M = 0.238", "h100 = 0.73", "n_s = 0.951",
@@ -87,7 +89,8 @@ def run_case(name, P, *, nside, info_extra="", mass=None, mask=None, particle_ma
     ini = "\n".join(lines) + "\n" + info_extra
     with open(os.path.join(d, "info.ini"), "w") as f:
         f.write(ini)
-    r = subprocess.run([REF_BIN, os.path.join(d, "info.ini"), os.path.join(d, "map.bin"),
+    binary = REF_BIN if law == "ann_nosom" else REF_BIN + "_" + law
+    r = subprocess.run([binary, os.path.join(d, "info.ini"), os.path.join(d, "map.bin"),
                         os.path.join(d, "par.txt")], capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"{name}: reference failed: {r.stderr[-500:]}")
@@ -97,7 +100,7 @@ def run_case(name, P, *, nside, info_extra="", mass=None, mask=None, particle_ma
     np.savez_compressed(
         os.path.join(HERE, name + ".npz"), map=mp, info=np.array(ini.replace(d, "@DIR@")),
         records=rec, mask=(np.asarray(mask, np.uint8) if mask is not None else np.zeros(0, np.uint8)),
-        **{"par_" + k: v for k, v in par.items()})
+        flux_law=np.array(law), **{"par_" + k: v for k, v in par.items()})
     assert np.all(np.isfinite(mp)), name
     print(f"{name}: nside={nside} n={len(P)} sum(map*dOmega)={mp.sum() * par['dOmega'][0]:.6e}")
 
@@ -142,6 +145,30 @@ def main():
     run_case("nside24", P, nside=24)
     P = synth.nfw_halo(1200, seed=109, n_sub=30, sub_frac=0.6)
     run_case("subhalo_ns128", P, nside=128)
+    # 8. the other flux laws (the reference links one getflux plugin per
+    #    build): velocity dispersions log-normal around 30 km/s, some below
+    #    the somv / somv2 saturation speeds of 1 and 5 km/s
+    P = synth.nfw_halo(900, seed=110, n_sub=3)
+    v_kms = np.exp(np.random.Generator(np.random.PCG64(1110)).normal(np.log(30.0), 1.6, len(P)))
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import oracle as O
+    op = O.make_params(nside=8, obs_pos=P.obs_pos, centerpos=P.centerpos, align_vec=P.align_vec,
+                       particle_masses=(P.particle_mass,))
+    vel_to_cgs = op.velocity_to_cgs
+    sigmav = (v_kms * 1.0e5 / vel_to_cgs).astype(np.float32)
+    for law in ("ann_somv", "ann_somv2", "ann_pwave", "decay"):
+        run_case("flux_" + law + "_ns32", P, nside=32, law=law, sigmav=sigmav, mem_buffer=400)
+    # adiabatic contraction in the reference's own units (r in kpc/h there)
+    Q = synth.nfw_halo(700, seed=111)
+    c = np.array([0.3612030, 0.2106580, 0.00687726])
+    scale = 1.0 / 40000.0
+    R = synth.Particles((Q.x * scale + c[0]).astype(np.float32), (Q.y * scale + c[1]).astype(np.float32),
+                        (Q.z * scale + c[2]).astype(np.float32), (Q.m * 1e-12).astype(np.float32),
+                        Q.rho, (Q.h * scale).astype(np.float32))
+    obs = tuple((np.array(Q.obs_pos) * scale + c).tolist())
+    run_case("flux_ann_adiabatic_ns16", R, nside=16, units="vl2", particle_masses=[4.1e-9],
+             obs=obs, centre=tuple(c.tolist()), align=(-0.025836, 0.133297, 0.990739),
+             law="ann_adiabatic")
 
 
 if __name__ == "__main__":

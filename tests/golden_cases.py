@@ -32,7 +32,8 @@ def load(name):
     info = parse_info(str(z["info"]))
     rec = z["records"]
     parts = {"m": rec[:, 0].copy(), "rho": rec[:, 1].copy(), "h": rec[:, 2].copy(),
-             "x": rec[:, 3].copy(), "y": rec[:, 4].copy(), "z": rec[:, 5].copy()}
+             "x": rec[:, 3].copy(), "y": rec[:, 4].copy(), "z": rec[:, 5].copy(),
+             "sigmav": rec[:, 9].copy()}
     mask = z["mask"]
     if mask.size:
         parts["rho"][mask == 0] = -1.0
@@ -40,7 +41,13 @@ def load(name):
         k = int(info["test"][0])
         parts = {k2: v[:k] for k2, v in parts.items()}
     par = {k[4:]: z[k] for k in z.files if k.startswith("par_")}
-    return {"parts": parts, "info": info, "map": z["map"], "par": par, "info_text": str(z["info"])}
+    law = str(z["flux_law"]) if "flux_law" in z.files else "ann_nosom"
+    return {"parts": parts, "info": info, "map": z["map"], "par": par, "info_text": str(z["info"]),
+            "flux_law": law}
+
+
+FLUX_LAWS = {"ann_nosom": 0, "ann_somv": 1, "ann_somv2": 2, "ann_pwave": 3, "decay": 4,
+             "ann_adiabatic": 5}
 
 
 def oracle_params(case):
@@ -52,4 +59,4 @@ def oracle_params(case):
         nside=int(info["nside"][0]), obs_pos=f("obs_pos"), centerpos=f("centerpos"),
         align_vec=f("align_vec"), h100=f("h100")[0], Omega_M=f("Omega_M")[0],
         Lbox_in_Mpc=f("Lbox_in_Mpc")[0], mass_to_Msun=f("mass_to_Msun", [-1.0])[0],
-        particle_masses=f("particle_masses"))
+        particle_masses=f("particle_masses"), flux_model=FLUX_LAWS[case["flux_law"]])

@@ -170,3 +170,16 @@ def test_reader_matches_golden_records():
     z = np.load(os.path.join(G.GOLDEN, "hires_mask_ns32.npz"))
     rec = z["records"]
     assert rec.shape[1] == 12 and rec.dtype == np.float32
+
+
+def test_flux_unit_factors_match_oracle():
+    import oracle as O
+    case = G.load("flux_decay_ns32")
+    p = O.make_params(nside=8, obs_pos=(1, 2, 3), centerpos=(0, 0, 0), align_vec=(0, 0, 1),
+                      particle_masses=(4.1e3,))
+    par = annmap.Parameters(text=case["info_text"].replace("@DIR@", "/x"))
+    assert par.flux_unit_factor(4) == p.decay_unit_factor
+    for law in (0, 1, 2, 3, 5):
+        assert par.flux_unit_factor(law) == p.unit_factor == par.unit_factor
+    with pytest.raises(ValueError):
+        par.flux_unit_factor(9)

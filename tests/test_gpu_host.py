@@ -59,3 +59,13 @@ def test_cpp_example_program_renders(tmp_path):
     assert math.isclose(d["total_flux"], ref.sum() * par.map.dOmega, rel_tol=1e-9)
     got, _ = read_healpix_map(fits)
     check(got, ref, COMP)
+
+
+@pytest.mark.parametrize("name", ["flux_ann_somv_ns32", "flux_ann_somv2_ns32", "flux_ann_pwave_ns32",
+                                  "flux_decay_ns32", "flux_ann_adiabatic_ns16"])
+def test_cpp_genmap_flux_laws(tmp_path, name):
+    import golden_cases as G
+    case, info = write_case(tmp_path, name, mem_buffer=250)
+    mp, total = host.genmap(info, COMP, flux_model=G.FLUX_LAWS[case["flux_law"]])
+    par = annmap.Parameters(info)
+    check(mp, case["map"], COMP, total=case["map"].sum() * par.map.dOmega, dOmega=par.map.dOmega)

@@ -64,7 +64,7 @@ def rend():
 def test_golden_maps(rend, name, precision):
     case = G.load(name)
     p = annmap.Parameters(text=case["info_text"].replace("@DIR@", "/x"))
-    rend.set_params(p)
+    rend.set_params(p, flux_model=case["flux_law"])
     got = rend.render(case["parts"], p.map.Nside, precision)
     ref = case["map"]
     st = rend.stats()
@@ -258,3 +258,14 @@ def test_render_batch_matches_single_renders(rend, device_maps):
         assert np.array_equal(g != 0, ref != 0)
         np.testing.assert_allclose(g, ref, rtol=1e-10, atol=0)
     rend.set_params(par0)
+
+
+def test_flux_law_needs_velocity_dispersion(rend):
+    case = G.load("flux_ann_somv_ns32")
+    p = annmap.Parameters(text=case["info_text"].replace("@DIR@", "/x"))
+    rend.set_params(p, flux_model="ann_somv")
+    parts = {k: v for k, v in case["parts"].items() if k != "sigmav"}
+    with pytest.raises(annmap.DmannError):
+        rend.render(parts, p.map.Nside, COMP)
+    rend.set_params(p)   # back to nosom: sigmav not needed
+    rend.render(parts, p.map.Nside, COMP)
