@@ -31,7 +31,7 @@ COMMON = ["-O3", "-std=c++17", "-lineinfo", "--expt-relaxed-constexpr", "-Xcompi
 # (source, fmad)
 CUDA_UNITS = [("prep.cu", False), ("disc_plain.cu", False), ("disc_comp.cu", True),
               ("capi.cu", True), ("noalloc.cu", True), ("adjoint.cu", False),
-              ("peaks.cu", True)]
+              ("peaks.cu", True), ("halocore.cu", False)]
 CXX_UNITS = ["frame.cpp"]
 
 LIB_DMANN = os.path.join(PKG, "libdmann.so")

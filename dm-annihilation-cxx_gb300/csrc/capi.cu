@@ -56,6 +56,10 @@ struct dmann_ctx {
     // workspace
     DevBuf in[7], theta, phi, ar, flux, cpix, key, queue, hist, ctr, fsum, acc, map;
     DevBuf cls, oacc, grad;   // the adjoint's class array, observer sums, staged gradient
+    // halo cores of the ann_core_nosom law (dmann_set_halo_cores)
+    DevBuf halo_f, halo_cells, corr;
+    HaloGrid halo{};
+    bool have_halos = false;
     dmann_stats stats{};
     bool stats_pending = false;
     long long *h_ctr = nullptr;   // pinned: C_COUNT counters, the flux sum, 12 adjoint sums
@@ -272,7 +276,8 @@ void dmann_destroy(dmann_ctx *ctx) {
                       &ctx->in[6],
                       &ctx->theta, &ctx->phi, &ctx->ar, &ctx->flux, &ctx->cpix, &ctx->key,
                       &ctx->queue, &ctx->hist, &ctx->ctr, &ctx->fsum, &ctx->acc, &ctx->map,
-                      &ctx->cls, &ctx->oacc, &ctx->grad};
+                      &ctx->cls, &ctx->oacc, &ctx->grad, &ctx->halo_f, &ctx->halo_cells,
+                      &ctx->corr};
     for (DevBuf *b : bufs)
         if (b->p) cudaFree(b->p);
     for (auto &kv : ctx->rings) {
@@ -339,7 +344,7 @@ dmann_status dmann_set_units(dmann_ctx *ctx, double unit_factor, double hires_th
     if (!ctx) return DMANN_ERR_INVALID;
     if (!(std::isfinite(unit_factor) && unit_factor > 0))
         return fail(ctx, DMANN_ERR_INVALID, "unit_factor must be finite and positive");
-    if (flux_model < DMANN_FLUX_ANN_NOSOM || flux_model > DMANN_FLUX_ANN_ADIABATIC)
+    if (flux_model < DMANN_FLUX_ANN_NOSOM || flux_model > DMANN_FLUX_ANN_CORE_NOSOM)
         return fail(ctx, DMANN_ERR_INVALID, "unknown flux model");
     ctx->unit_factor = unit_factor;
     ctx->hires = hires_threshold;
@@ -370,6 +375,103 @@ dmann_status dmann_set_flux_params(dmann_ctx *ctx, double velocity_to_cgs, const
         return fail(ctx, DMANN_ERR_INVALID, "non-finite flux parameter");
     ctx->vel_to_cgs = velocity_to_cgs;
     std::memcpy(ctx->fcpos, cpos, sizeof(double) * 3);
+    return DMANN_OK;
+}
+
+dmann_status dmann_set_halo_cores(dmann_ctx *ctx, const float *x, const float *y, const float *z,
+                                  const float *radius, int n_halos) {
+    if (!ctx) return DMANN_ERR_INVALID;
+    if (n_halos < 0 || (n_halos > 0 && (!x || !y || !z || !radius)))
+        return fail(ctx, DMANN_ERR_INVALID, "bad halo arrays");
+    CK(cudaSetDevice(ctx->device));
+    const int n = n_halos;
+    // core radius in box units, held in a float as the reference passes it
+    // (halocore.cpp:62-66: radius / (0.73 * 40000.0) into a float parameter)
+    std::vector<float> r(n);
+    float rmax = 0.0f;
+    float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    const float *c[3] = {x, y, z};
+    for (int i = 0; i < n; i++) {
+        r[i] = (float)((double)radius[i] / (0.73 * 40000.0));
+        if (!std::isfinite(r[i]) || !std::isfinite(x[i]) || !std::isfinite(y[i]) || !std::isfinite(z[i]))
+            return fail(ctx, DMANN_ERR_INVALID, "non-finite halo");
+        rmax = std::max(rmax, r[i]);
+        for (int k = 0; k < 3; k++) {
+            lo[k] = std::min(lo[k], c[k][i]);
+            hi[k] = std::max(hi[k], c[k][i]);
+        }
+    }
+    HaloGrid gr{};
+    gr.n_halos = n;
+    if (n == 0 || !(rmax > 0.0f)) {   // no halo can contain a particle
+        gr.nx = gr.ny = gr.nz = 1;
+        gr.ox = gr.oy = gr.oz = 0.0f;
+        gr.inv_cell = 0.0f;
+        std::vector<int> cs(2, 0);
+        dmann_status st = ensure(ctx, ctx->halo_cells, sizeof(int) * 2);
+        if (st != DMANN_OK) return st;
+        CK(cudaMemcpy(ctx->halo_cells.p, cs.data(), sizeof(int) * 2, cudaMemcpyHostToDevice));
+        gr.cell_start = (const int *)ctx->halo_cells.p;
+        gr.nx = 0;   // every particle falls outside
+        ctx->halo = gr;
+        ctx->have_halos = true;
+        return DMANN_OK;
+    }
+    // cells of at least the largest radius (with a margin for the rounding
+    // of a particle's cell index), at most 256 per axis
+    float cell = rmax * 1.001f + 1e-30f;
+    int dims[3];
+    for (;;) {
+        bool ok = true;
+        for (int k = 0; k < 3; k++) {
+            const double ext = (double)hi[k] - lo[k] + 2.0 * cell;
+            dims[k] = (int)std::ceil(ext / cell) + 1;
+            if (dims[k] > 256) ok = false;
+        }
+        if (ok) break;
+        cell *= 1.5f;
+    }
+    gr.ox = lo[0] - cell;
+    gr.oy = lo[1] - cell;
+    gr.oz = lo[2] - cell;
+    gr.inv_cell = 1.0f / cell;
+    gr.nx = dims[0];
+    gr.ny = dims[1];
+    gr.nz = dims[2];
+    const size_t ncell = (size_t)dims[0] * dims[1] * dims[2];
+    std::vector<int> cid(n), cs(ncell + 1, 0);
+    for (int i = 0; i < n; i++) {
+        int k3[3];
+        const float o[3] = {gr.ox, gr.oy, gr.oz};
+        for (int k = 0; k < 3; k++)
+            k3[k] = std::min(dims[k] - 1, std::max(0, (int)((c[k][i] - o[k]) * gr.inv_cell)));
+        cid[i] = (k3[2] * dims[1] + k3[1]) * dims[0] + k3[0];
+        cs[cid[i] + 1]++;
+    }
+    for (size_t k = 0; k < ncell; k++) cs[k + 1] += cs[k];
+    std::vector<float> hf(4 * (size_t)n);
+    std::vector<int> fill(cs.begin(), cs.end() - 1);
+    for (int i = 0; i < n; i++) {   // halos of a cell keep the table's order
+        const int at = fill[cid[i]]++;
+        hf[at] = x[i];
+        hf[n + at] = y[i];
+        hf[2 * (size_t)n + at] = z[i];
+        hf[3 * (size_t)n + at] = r[i];
+    }
+    dmann_status st;
+    if ((st = ensure(ctx, ctx->halo_f, sizeof(float) * hf.size())) ||
+        (st = ensure(ctx, ctx->halo_cells, sizeof(int) * cs.size())))
+        return st;
+    CK(cudaMemcpy(ctx->halo_f.p, hf.data(), sizeof(float) * hf.size(), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(ctx->halo_cells.p, cs.data(), sizeof(int) * cs.size(), cudaMemcpyHostToDevice));
+    const float *f = (const float *)ctx->halo_f.p;
+    gr.hx = f;
+    gr.hy = f + n;
+    gr.hz = f + 2 * (size_t)n;
+    gr.hr = f + 3 * (size_t)n;
+    gr.cell_start = (const int *)ctx->halo_cells.p;
+    ctx->halo = gr;
+    ctx->have_halos = true;
     return DMANN_OK;
 }
 
@@ -532,6 +634,13 @@ dmann_status dmann_map_add_v(dmann_ctx *ctx, const float *x, const float *y, con
     CK(cudaMemsetAsync((long long *)ctx->ctr.p + kCtrChunkFirst, 0, 8 * (C_COUNT - kCtrChunkFirst), s));
     PrepArgs pa;
     pa.p = {dev[0], dev[1], dev[2], dev[3], dev[4], dev[5], (int)N, dev[6]};
+    pa.core_corr = nullptr;
+    if (ctx->flux_model == DMANN_FLUX_ANN_CORE_NOSOM) {
+        if (!ctx->have_halos) return fail(ctx, DMANN_ERR_STATE, "halo cores not set (dmann_set_halo_cores)");
+        if ((st = ensure(ctx, ctx->corr, 8 * N)) != DMANN_OK) return st;
+        CK(launch_halo_core(ctx->halo, pa.p, (double *)ctx->corr.p, s));
+        pa.core_corr = (const double *)ctx->corr.p;
+    }
     pa.f = f;
     pa.g = ctx->g;
     pa.out = {(double *)ctx->theta.p, (double *)ctx->phi.p, (double *)ctx->ar.p,
@@ -645,6 +754,7 @@ dmann_status issue_observer(dmann_ctx *ctx, const float *const dev[6], int n, in
         CK(cudaMemsetAsync(ctx->hist.p, 0, 4 * (size_t)kKeys, s));
         PrepArgs pa;
         pa.p = {dev[0], dev[1], dev[2], dev[3], dev[4], dev[5], n};
+        pa.core_corr = (const double *)ctx->corr.p;   // filled once per batch (core law)
         pa.f = f;
         pa.g = ctx->g;
         pa.out = {(double *)ctx->theta.p, (double *)ctx->phi.p, (double *)ctx->ar.p,
@@ -729,6 +839,12 @@ dmann_status dmann_render_batch(dmann_ctx *ctx, const float *x, const float *y, 
             CK(cudaMemcpyAsync(ctx->in[k].p, src[k], 4 * N, cudaMemcpyHostToDevice, s));
             dev[k] = (const float *)ctx->in[k].p;
         }
+    }
+    if (ctx->flux_model == DMANN_FLUX_ANN_CORE_NOSOM) {   // observer-independent: once
+        if (!ctx->have_halos) return fail(ctx, DMANN_ERR_STATE, "halo cores not set (dmann_set_halo_cores)");
+        if ((st = ensure(ctx, ctx->corr, 8 * n1)) != DMANN_OK) return st;
+        Particles pp = {dev[0], dev[1], dev[2], dev[3], dev[4], dev[5], (int)N};
+        CK(launch_halo_core(ctx->halo, pp, (double *)ctx->corr.p, s));
     }
     std::vector<char> on_dev(n_obs);
     bool all_dev = true;
@@ -850,6 +966,7 @@ dmann_status dmann_adjoint(dmann_ctx *ctx, const float *x, const float *y, const
     pa.precision = DMANN_PLAIN_F64;
     pa.block_bucket_min = bmin;
     pa.deposit_singles = 0;
+    pa.core_corr = nullptr;
     CK(launch_prep(pa, s));
     CK(launch_scan(pa.hist, pa.ctr, bmin, s));
     CK(launch_scatter(pa, (int *)ctx->queue.p, s));
@@ -930,7 +1047,7 @@ dmann_status dmann_code_units(double h100, double Lbox_in_Mpc, double mass_to_Ms
 
 dmann_status dmann_flux_unit_factor(int flux_model, double h100, double Lbox_in_Mpc,
                                     double mass_to_Msun, double *unit_factor) {
-    if (!unit_factor || flux_model < DMANN_FLUX_ANN_NOSOM || flux_model > DMANN_FLUX_ANN_ADIABATIC)
+    if (!unit_factor || flux_model < DMANN_FLUX_ANN_NOSOM || flux_model > DMANN_FLUX_ANN_CORE_NOSOM)
         return DMANN_ERR_INVALID;
     CodeUnits u;
     setup_units(h100, Lbox_in_Mpc, mass_to_Msun, &u);

@@ -48,6 +48,15 @@ struct Accum {
     float *hi, *lo;     // DMANN_COMP_F32 (compensated two-float planes)
 };
 
+// Halo cores of the ann_core_nosom law, bucketed into a uniform grid whose
+// cell is at least the largest core radius (halocore.cu).
+struct HaloGrid {
+    const float *hx, *hy, *hz, *hr;   // centres and radii (box units), sorted by cell
+    const int *cell_start;            // [nx*ny*nz + 1], x fastest
+    float ox, oy, oz, inv_cell;       // grid origin and 1 / cell size
+    int nx, ny, nz, n_halos;
+};
+
 struct PrepArgs {
     Particles p;
     Frame f;
@@ -60,6 +69,7 @@ struct PrepArgs {
     int precision;
     int block_bucket_min;       // discs whose size bucket >= this go block-per-particle
     int deposit_singles;        // 0: classify only (the adjoint), no map deposits
+    const double *core_corr;    // per-particle halo-core factor r (ann_core_nosom law)
 };
 
 struct DiscArgs {
@@ -79,6 +89,8 @@ cudaError_t launch_scan(int *hist, long long *ctr, int block_bucket_min, cudaStr
 cudaError_t launch_scatter(const PrepArgs &a, int *queue, cudaStream_t s);
 cudaError_t launch_finalize(const Accum &acc, int precision, int npix, double dOmega,
                             double scale, double *out, int accumulate, cudaStream_t s);
+// halocore.cu: corr[i] = the halo-core factor r of particle i
+cudaError_t launch_halo_core(const HaloGrid &g, const Particles &p, double *corr, cudaStream_t s);
 // disc_plain.cu / disc_comp.cu
 // Launch the block-per-particle kernel, record `mid` (if not null), then the
 // warp-per-particle kernel.

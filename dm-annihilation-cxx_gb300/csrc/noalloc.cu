@@ -223,6 +223,7 @@ extern "C" dmann_status dmann_render_noalloc(const float *x, const float *y, con
         pa.precision = DMANN_COMP_F32;
         pa.block_bucket_min = 11;  // discs estimated above 1024 pixels: block per disc
         pa.deposit_singles = 1;
+        pa.core_corr = nullptr;
         NA_CK(launch_prep(pa, s));
         NA_CK(launch_scan(pa.hist, pa.ctr, pa.block_bucket_min, s));
         NA_CK(launch_scatter(pa, (int *)(b + L.queue), s));

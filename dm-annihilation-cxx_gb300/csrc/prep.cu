@@ -87,6 +87,10 @@ __device__ inline double particle_flux(const PrepArgs &a, int i, float mass, flo
         fluxes *= (factor * factor);
         return fluxes;
     }
+    case 6: {  // flux_ann_core_nosom.cpp:9-17: the halo-core factor squared
+        const double r = a.core_corr[i];
+        return r * r * uf * (double)dens * (double)mass / (4.0 * kPi * d * d);
+    }
     default:   // flux_ann_nosom.cpp:18
         return uf * (double)dens * (double)mass / (4.0 * kPi * d * d);
     }

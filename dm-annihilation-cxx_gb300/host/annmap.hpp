@@ -158,6 +158,9 @@ public:
 
     void start();
     void saveToFits(const std::string &fits_file, bool isVerbose = false);
+    // The halo table the ann_core_nosom law reads (default as the reference:
+    // ./halocore/VL2_Halos.data, relative to the working directory).
+    void setHaloFile(const std::string &path) { halo_file_ = path; }
     bool isFinished() const { return isFinished_; }
     MAPTYPE *getMap() { return map_; }
     int getNside() const { return par_->map.Nside; }
@@ -172,7 +175,15 @@ private:
     MAPTYPE *map_ = nullptr;
     double total_flux_ = 0;
     dmann_stats stats_{};
+    std::string halo_file_ = "./halocore/VL2_Halos.data";
 };
+
+// The ann_core_nosom law's halo table (src/halocore/halocore.cpp:16-45): one
+// halo per line, x y z radius.  Throws on an empty or short file.
+struct HaloTable {
+    std::vector<float> x, y, z, radius;
+};
+HaloTable readHaloTable(const std::string &path);
 
 // HEALPix FITS map (the layout of write_Healpix_map_to_fits with FP64 data:
 // empty primary HDU, one BINTABLE with column "signal").

@@ -77,10 +77,12 @@ int64_t annmap_read_native(const char *path, const char *maskfile, int test, int
 // The reference's main flow (src/main.cpp:35-66) on the GPU: Parameters,
 // DataReader (test limit and buffer from the info file), MapGenerator::start,
 // and saveToFits to the info file's outputmap when it names one, with the
-// flux law flux_model (dmann_flux).  map_out
+// flux law flux_model (dmann_flux; halo_file for the core law, NULL or ""
+// for the reference's default path).  map_out
 // receives the 12 nside^2 map (npix must match); total_flux the "Total Conts".
 int annmap_genmap(const char *info_file, int precision, int device, int flux_model,
-                  double *map_out, int64_t npix, double *total_flux, char *err, int errlen) {
+                  const char *halo_file, double *map_out, int64_t npix, double *total_flux,
+                  char *err, int errlen) {
     try {
         annmap::Parameters par(info_file);
         if (!par.isNative) return fail(err, errlen, "only native particle files are supported");
@@ -90,6 +92,7 @@ int annmap_genmap(const char *info_file, int precision, int device, int flux_mod
         reader.setBuf((unsigned)par.memParts);
         reader.open();
         annmap::MapGenerator gen(&par, &reader, precision, device, flux_model);
+        if (halo_file && *halo_file) gen.setHaloFile(halo_file);
         gen.start();
         reader.close();
         std::memcpy(map_out, gen.getMap(), sizeof(double) * (size_t)npix);

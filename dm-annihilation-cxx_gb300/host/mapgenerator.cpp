@@ -14,6 +14,8 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <fstream>
+#include <sstream>
 #include <stdexcept>
 #include <string>
 #include <sys/stat.h>
@@ -79,6 +81,11 @@ void MapGenerator::start() {
     ctx.check(dmann_set_units(ctx.c, par_->fluxUnitFactor(flux_model_), par_->hiresThreshold(),
                               flux_model_));
     ctx.check(dmann_set_flux_params(ctx.c, par_->codeunits.velocity_to_cgs, par_->params.cpos));
+    if (flux_model_ == DMANN_FLUX_ANN_CORE_NOSOM) {
+        const HaloTable t = readHaloTable(halo_file_);
+        ctx.check(dmann_set_halo_cores(ctx.c, t.x.data(), t.y.data(), t.z.data(), t.radius.data(),
+                                       (int)t.x.size()));
+    }
     cuda_check(cudaSetDevice(device_), "cudaSetDevice");
     cudaStream_t s = nullptr;
     cuda_check(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking), "stream");
@@ -134,6 +141,32 @@ void MapGenerator::start() {
     ctx.check(dmann_get_stats(ctx.c, &stats_));
     total_flux_ = stats_.total_flux;
     isFinished_ = true;
+}
+
+HaloTable readHaloTable(const std::string &path) {
+    std::ifstream f(path);
+    if (!f.is_open()) throw std::runtime_error("cannot open halo file " + path);
+    HaloTable t;
+    std::string line;
+    size_t lines = 0;
+    std::string all;
+    while (std::getline(f, line)) {
+        lines++;
+        all += line;
+        all += ' ';
+    }
+    if (lines == 0) throw std::runtime_error("empty halo file " + path);
+    std::istringstream in(all);
+    for (size_t i = 0; i < lines; i++) {
+        float v[4];
+        for (int k = 0; k < 4; k++)
+            if (!(in >> v[k])) throw std::runtime_error("halo file " + path + ": short record");
+        t.x.push_back(v[0]);
+        t.y.push_back(v[1]);
+        t.z.push_back(v[2]);
+        t.radius.push_back(v[3]);
+    }
+    return t;
 }
 
 void MapGenerator::saveToFits(const std::string &fits_file, bool isVerbose) {

@@ -16,8 +16,10 @@ OK, ERR_INVALID, ERR_CUDA, ERR_NOMEM, ERR_STATE, ERR_TIMEOUT, ERR_NODEVICE, ERR_
 STATUS_NAMES = {0: "OK", 1: "INVALID", 2: "CUDA", 3: "NOMEM", 4: "STATE", 5: "TIMEOUT", 6: "NODEVICE",
                 7: "TOO_LARGE"}
 PLAIN_F64, COMP_F32 = 0, 1
-FLUX_ANN_NOSOM, FLUX_ANN_SOMV, FLUX_ANN_SOMV2, FLUX_ANN_PWAVE, FLUX_DECAY, FLUX_ANN_ADIABATIC = range(6)
-FLUX_LAWS = {"ann_nosom": 0, "ann_somv": 1, "ann_somv2": 2, "ann_pwave": 3, "decay": 4, "ann_adiabatic": 5}
+(FLUX_ANN_NOSOM, FLUX_ANN_SOMV, FLUX_ANN_SOMV2, FLUX_ANN_PWAVE, FLUX_DECAY, FLUX_ANN_ADIABATIC,
+ FLUX_ANN_CORE_NOSOM) = range(7)
+FLUX_LAWS = {"ann_nosom": 0, "ann_somv": 1, "ann_somv2": 2, "ann_pwave": 3, "decay": 4, "ann_adiabatic": 5,
+             "ann_core_nosom": 6}
 
 
 class DmannError(RuntimeError):
@@ -69,6 +71,7 @@ SIGNATURES = {
     "dmann_map_add_v": (C.c_int, [_P, _P, _P, _P, _P, _P, _P, _P, C.c_int64]),
     "dmann_render_v": (C.c_int, [_P, _P, _P, _P, _P, _P, _P, _P, C.c_int64, C.c_int, C.c_int, _P, C.c_int]),
     "dmann_set_flux_params": (C.c_int, [_P, C.c_double, _D3]),
+    "dmann_set_halo_cores": (C.c_int, [_P, _P, _P, _P, _P, C.c_int]),
     "dmann_flux_unit_factor": (C.c_int, [C.c_int, C.c_double, C.c_double, C.c_double, _D3]),
     "dmann_get_stats": (C.c_int, [_P, C.POINTER(Stats)]),
     "dmann_render_batch": (C.c_int, [_P, _P, _P, _P, _P, _P, _P, C.c_int64, C.c_int, _D3, _D3,

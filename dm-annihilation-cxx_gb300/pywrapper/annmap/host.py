@@ -25,8 +25,8 @@ def load():
         L.annmap_read_native.argtypes = [C.c_char_p, C.c_char_p, C.c_int, C.c_int,
                                          C.POINTER(C.c_float), C.c_int64, C.c_char_p, C.c_int]
         L.annmap_read_native.restype = C.c_int64
-        L.annmap_genmap.argtypes = [C.c_char_p, C.c_int, C.c_int, C.c_int, D, C.c_int64, D, C.c_char_p,
-                                    C.c_int]
+        L.annmap_genmap.argtypes = [C.c_char_p, C.c_int, C.c_int, C.c_int, C.c_char_p, D, C.c_int64, D,
+                                    C.c_char_p, C.c_int]
         L.annmap_genmap.restype = C.c_int
         L.annmap_write_fits.argtypes = [C.c_char_p, D, C.c_int64, C.c_char_p, C.c_int]
         L.annmap_write_fits.restype = C.c_int
@@ -63,7 +63,7 @@ def read_native(path: str, maskfile: str = "", test: int = -1, buf: int = 100000
 
 
 def genmap(info_file: str, precision: int = 1, device: int = 0, nside: int = None,
-           flux_model: int = 0) -> tuple:
+           flux_model: int = 0, halo_file: str = "") -> tuple:
     """The reference's main flow in C++ (Parameters, DataReader, MapGenerator,
     saveToFits when the info file names an output map).  Returns (map, total flux)."""
     if nside is None:
@@ -72,7 +72,7 @@ def genmap(info_file: str, precision: int = 1, device: int = 0, nside: int = Non
     tot = C.c_double()
     e = _err()
     if load().annmap_genmap(info_file.encode(), int(precision), int(device), int(flux_model),
-                            mp.ctypes.data_as(C.POINTER(C.c_double)), mp.size, C.byref(tot), e, 512) != 0:
+                            halo_file.encode(), mp.ctypes.data_as(C.POINTER(C.c_double)), mp.size, C.byref(tot), e, 512) != 0:
         raise RuntimeError(e.value.decode())
     return mp, tot.value
 

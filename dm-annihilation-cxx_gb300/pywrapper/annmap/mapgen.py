@@ -101,6 +101,12 @@ class Renderer:
         self._check(self.L.dmann_set_flux_params(self.ctx, float(velocity_to_cgs),
                                                  (C.c_double * 3)(*[float(v) for v in cpos])))
 
+    def set_halo_cores(self, x, y, z, radius):
+        """The ann_core_nosom law's halo table (annmap.halocore.read_halo_table)."""
+        arrs = [np.ascontiguousarray(a, dtype=np.float32) for a in (x, y, z, radius)]
+        n = len(arrs[0])
+        self._check(self.L.dmann_set_halo_cores(self.ctx, *[C.c_void_p(a.ctypes.data) for a in arrs], n))
+
     def set_params(self, par, flux_model: int = 0):
         """Frame, units and flux law from a Parameters object (flux_model is
         a dmann_flux value or a law name such as "ann_somv")."""
@@ -245,12 +251,14 @@ class Renderer:
 class MapGenerator:
     """The reference's MapGenerator (src/mapgenerator.h:8-26) on the GPU."""
 
-    def __init__(self, par, reader, precision: int = COMP_F32, device: int = 0, flux_model=0):
+    def __init__(self, par, reader, precision: int = COMP_F32, device: int = 0, flux_model=0,
+                 halo_file: str = "./halocore/VL2_Halos.data"):
         self.par_ = par
         self.reader_ = reader
         self.precision = precision
         self.device = device
         self.flux_model = flux_model   # the reference's link-time getflux plugin, chosen here
+        self.halo_file = halo_file     # read by the ann_core_nosom law, as the reference does
         self.map_ = None
         self.isFinished_ = False
         self.total_flux = None
@@ -259,6 +267,9 @@ class MapGenerator:
         r = Renderer(self.device)
         try:
             r.set_params(self.par_, self.flux_model)
+            if self.flux_model in (6, "ann_core_nosom"):
+                from .halocore import read_halo_table
+                r.set_halo_cores(*read_halo_table(self.halo_file))
             r.begin(self.par_.map.Nside, self.precision)
             while self.reader_.hasNext():
                 r.add(self.reader_.next_chunk())

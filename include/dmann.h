@@ -83,8 +83,11 @@ typedef enum {
     DMANN_FLUX_ANN_SOMV2 = 2,     /* x (c / max(v, 5))^2 / 1e8       flux_ann_somv2.cpp */
     DMANN_FLUX_ANN_PWAVE = 3,     /* x (sigmav velocity_to_cgs / c)^2 flux_ann_pwave.cpp */
     DMANN_FLUX_DECAY = 4,         /* unit_factor m / (4 pi d^2)      flux_decay.cpp */
-    DMANN_FLUX_ANN_ADIABATIC = 5  /* nosom x f(r)^2, r = |pos - cpos| * 40000
+    DMANN_FLUX_ANN_ADIABATIC = 5, /* nosom x f(r)^2, r = |pos - cpos| * 40000
                                      (kpc/h in the reference's units) flux_ann_adiabatic.cpp */
+    DMANN_FLUX_ANN_CORE_NOSOM = 6 /* nosom x r^2, r the halo-core factor of the
+                                     halos set by dmann_set_halo_cores
+                                     flux_ann_core_nosom.cpp, halocore/halocore.cpp */
 } dmann_flux;
 
 /* Counters of the last dmann_render call on a context. */
@@ -160,6 +163,15 @@ dmann_status dmann_get_tuning(const dmann_ctx *ctx, dmann_tuning *t);
  * the entry.  dmann_get_tuning_nside returns the tuning in force for nside. */
 dmann_status dmann_set_tuning_nside(dmann_ctx *ctx, int nside, const dmann_tuning *t);
 dmann_status dmann_get_tuning_nside(const dmann_ctx *ctx, int nside, dmann_tuning *t);
+
+/* The halo table of the ann_core_nosom law (src/halocore/halocore.cpp:
+ * the VL2_Halos.data columns x y z radius, one halo per line): centres in
+ * box units, radius in the table's units (the core radius is
+ * radius / (0.73 * 40000) box units).  Each particle's factor is the product
+ * over the halos whose core contains it of 0.55 (d / R)^-0.9.  Copied to the
+ * device; n_halos = 0 makes every factor 1. */
+dmann_status dmann_set_halo_cores(dmann_ctx *ctx, const float *x, const float *y,
+                                  const float *z, const float *radius, int n_halos);
 
 /* ---- rendering ---- */
 /* Projects n particles (float32 SoA: positions x,y,z, mass m, density rho,

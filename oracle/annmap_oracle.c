@@ -154,6 +154,30 @@ typedef struct {
     int kept;
 } geom_t;
 
+/* src/halocore/halocore.cpp:70-83 coreFunc: arguments arrive as floats */
+static double core_func(float x, float y, float z, float hxc, float hyc, float hzc,
+                        float radius) {
+    double xx = (x - hxc);
+    double yy = (y - hyc);
+    double zz = (z - hzc);
+    double r = sqrt(xx * xx + yy * yy + zz * zz);
+    double ratio = 1.0;
+    if (r < radius) {
+        if (r > 0) ratio = 0.55 * pow(r / radius, -0.9);
+    }
+    return ratio;
+}
+
+/* src/halocore/halocore.cpp:52-67 getCorrection, halos in file order */
+static double core_correction(const orc_params *p, float x, float y, float z) {
+    double xp = x, yp = y, zp = z;
+    double r = 1.0;
+    for (int i = 0; i < p->n_halos; i++)
+        r *= core_func((float)xp, (float)yp, (float)zp, p->halo_x[i], p->halo_y[i], p->halo_z[i],
+                       (float)(p->halo_r[i] / (0.73 * 40000.0)));
+    return r;
+}
+
 /* getflux of the flux law p->flux_model for one particle at distance d, each
  * in the operation order of its plugin (sigmav only read by the laws that
  * use it). */
@@ -193,6 +217,10 @@ static double orc_flux(const orc_params *p, double mass, double dens, double sig
         double fluxes = uf * dens * mass / (4.0 * PI * d * d);
         fluxes *= (factor * factor);
         return fluxes;
+    }
+    case ORC_FLUX_CORE_NOSOM: { /* src/flux/flux_ann_core_nosom.cpp:9-17 */
+        double r = core_correction(p, (float)px, (float)py, (float)pz);
+        return r * r * uf * dens * mass / (4.0 * PI * d * d);
     }
     default: /* src/flux/flux_ann_nosom.cpp:12-23 */
         return uf * dens * mass / (4.0 * PI * d * d);

@@ -83,11 +83,15 @@ typedef struct {
      * link-time getflux plugins in the src/flux directory, see orc_flux */
     int flux_model;
     double decay_unit_factor; /* flux_decay.cpp:10-13 (derived) */
+    /* halo table of the ann_core_nosom law (halocore.cpp: x y z radius per
+     * line, in file order; not owned) */
+    const float *halo_x, *halo_y, *halo_z, *halo_r;
+    int n_halos;
 } orc_params;
 
 /* Flux laws, in the numbering of the C ABI's dmann_flux. */
 enum { ORC_FLUX_NOSOM = 0, ORC_FLUX_SOMV = 1, ORC_FLUX_SOMV2 = 2, ORC_FLUX_PWAVE = 3,
-       ORC_FLUX_DECAY = 4, ORC_FLUX_ADIABATIC = 5 };
+       ORC_FLUX_DECAY = 4, ORC_FLUX_ADIABATIC = 5, ORC_FLUX_CORE_NOSOM = 6 };
 
 /* Fills every derived field from the inputs (setupUnits, setupParams,
  * setupRotation, setNside and the per-map constants of genmap.cpp). */

@@ -42,6 +42,8 @@ class OrcParams(C.Structure):
         ("unit_factor", C.c_double), ("hires_threshold", C.c_double),
         ("npix", C.c_int64), ("dOmega", C.c_double), ("theta0", C.c_double),
         ("flux_model", C.c_int), ("decay_unit_factor", C.c_double),
+        ("halo_x", C.POINTER(C.c_float)), ("halo_y", C.POINTER(C.c_float)),
+        ("halo_z", C.POINTER(C.c_float)), ("halo_r", C.POINTER(C.c_float)), ("n_halos", C.c_int),
     ]
 
 
@@ -154,9 +156,16 @@ class Healpix:
 # ---------------------------------------------------------------- params
 def make_params(*, nside, obs_pos, centerpos, align_vec, h100=0.73, Omega_M=0.238,
                 Lbox_in_Mpc=0.001, mass_to_Msun=1.0, particle_masses=(0.0,),
-                redshift=0.0, flux_model=0) -> OrcParams:
+                redshift=0.0, flux_model=0, halos=None) -> OrcParams:
+    """halos: optional (x, y, z, radius) arrays of the ann_core_nosom law's
+    halo table (kept alive on the returned object)."""
     p = OrcParams()
     p.flux_model = int(flux_model)
+    if halos is not None:
+        arrs = [np.ascontiguousarray(a, dtype=np.float32) for a in halos]
+        p._halos = arrs
+        p.halo_x, p.halo_y, p.halo_z, p.halo_r = [a.ctypes.data_as(C.POINTER(C.c_float)) for a in arrs]
+        p.n_halos = len(arrs[0])
     p.h100, p.Omega_M, p.Lbox_in_Mpc, p.mass_to_Msun, p.redshift = (
         h100, Omega_M, Lbox_in_Mpc, mass_to_Msun, redshift)
     for i in range(3):
@@ -261,6 +270,8 @@ def with_observer(p: OrcParams, obs_pos) -> OrcParams:
     """A copy of p with another observer position (all derived fields redone)."""
     q = OrcParams()
     C.memmove(C.byref(q), C.byref(p), C.sizeof(OrcParams))
+    if hasattr(p, "_halos"):
+        q._halos = p._halos
     for i in range(3):
         q.obs_pos[i] = float(obs_pos[i])
     lib().orc_params_setup(C.byref(q))

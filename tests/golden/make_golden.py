@@ -61,8 +61,13 @@ def parse_params(text):
 
 def run_case(name, P, *, nside, info_extra="", mass=None, mask=None, particle_masses=None,
              obs=None, centre=(0.0, 0.0, 0.0), align=(0.0, 0.0, 1.0), units="kpc",
-             mem_buffer=1000, test=None, law="ann_nosom", sigmav=None):
+             mem_buffer=1000, test=None, law="ann_nosom", sigmav=None, halos=None):
     d = tempfile.mkdtemp(prefix="golden_")
+    if halos is not None:   # the core law reads ./halocore/VL2_Halos.data (x y z radius lines)
+        os.makedirs(os.path.join(d, "halocore"))
+        with open(os.path.join(d, "halocore", "VL2_Halos.data"), "w") as f:
+            for row in np.stack(halos, axis=1):
+                f.write("\t".join(repr(float(np.float32(v))) for v in row) + "\n")
     rec = write_native(os.path.join(d, "parts.bin"), P, extra_mass=mass, sigmav=sigmav)
     obs = P.obs_pos if obs is None else obs
     pm = particle_masses if particle_masses is not None else [P.particle_mass]
@@ -91,7 +96,7 @@ def run_case(name, P, *, nside, info_extra="", mass=None, mask=None, particle_ma
         f.write(ini)
     binary = REF_BIN if law == "ann_nosom" else REF_BIN + "_" + law
     r = subprocess.run([binary, os.path.join(d, "info.ini"), os.path.join(d, "map.bin"),
-                        os.path.join(d, "par.txt")], capture_output=True, text=True)
+                        os.path.join(d, "par.txt")], capture_output=True, text=True, cwd=d)
     if r.returncode != 0:
         raise RuntimeError(f"{name}: reference failed: {r.stderr[-500:]}")
     mp = np.fromfile(os.path.join(d, "map.bin"), np.float64)
@@ -100,7 +105,9 @@ def run_case(name, P, *, nside, info_extra="", mass=None, mask=None, particle_ma
     np.savez_compressed(
         os.path.join(HERE, name + ".npz"), map=mp, info=np.array(ini.replace(d, "@DIR@")),
         records=rec, mask=(np.asarray(mask, np.uint8) if mask is not None else np.zeros(0, np.uint8)),
-        flux_law=np.array(law), **{"par_" + k: v for k, v in par.items()})
+        flux_law=np.array(law),
+        halos=(np.stack(halos, axis=1).astype(np.float32) if halos is not None else np.zeros((0, 4), np.float32)),
+        **{"par_" + k: v for k, v in par.items()})
     assert np.all(np.isfinite(mp)), name
     print(f"{name}: nside={nside} n={len(P)} sum(map*dOmega)={mp.sum() * par['dOmega'][0]:.6e}")
 
@@ -169,6 +176,16 @@ def main():
     run_case("flux_ann_adiabatic_ns16", R, nside=16, units="vl2", particle_masses=[4.1e-9],
              obs=obs, centre=tuple(c.tolist()), align=(-0.025836, 0.133297, 0.990739),
              law="ann_adiabatic")
+    # halo cores (VL2_Halos.data layout: x y z radius) on 300 synthetic halos
+    # centred on particles, radius column 1..8 (core radius radius/29200 box units)
+    rng = np.random.Generator(np.random.PCG64(1112))
+    pick = rng.choice(len(R), 300, replace=False)
+    jit = rng.normal(0.0, 5e-5, (300, 3))
+    halos = ((R.x[pick] + jit[:, 0]).astype(np.float32), (R.y[pick] + jit[:, 1]).astype(np.float32),
+             (R.z[pick] + jit[:, 2]).astype(np.float32), rng.uniform(1.0, 8.0, 300).astype(np.float32))
+    run_case("flux_ann_core_nosom_ns16", R, nside=16, units="vl2", particle_masses=[4.1e-9],
+             obs=obs, centre=tuple(c.tolist()), align=(-0.025836, 0.133297, 0.990739),
+             law="ann_core_nosom", halos=halos)
 
 
 if __name__ == "__main__":

@@ -42,12 +42,13 @@ def load(name):
         parts = {k2: v[:k] for k2, v in parts.items()}
     par = {k[4:]: z[k] for k in z.files if k.startswith("par_")}
     law = str(z["flux_law"]) if "flux_law" in z.files else "ann_nosom"
+    halos = z["halos"] if "halos" in z.files else np.zeros((0, 4), np.float32)
     return {"parts": parts, "info": info, "map": z["map"], "par": par, "info_text": str(z["info"]),
-            "flux_law": law}
+            "flux_law": law, "halos": halos}
 
 
 FLUX_LAWS = {"ann_nosom": 0, "ann_somv": 1, "ann_somv2": 2, "ann_pwave": 3, "decay": 4,
-             "ann_adiabatic": 5}
+             "ann_adiabatic": 5, "ann_core_nosom": 6}
 
 
 def oracle_params(case):
@@ -59,4 +60,5 @@ def oracle_params(case):
         nside=int(info["nside"][0]), obs_pos=f("obs_pos"), centerpos=f("centerpos"),
         align_vec=f("align_vec"), h100=f("h100")[0], Omega_M=f("Omega_M")[0],
         Lbox_in_Mpc=f("Lbox_in_Mpc")[0], mass_to_Msun=f("mass_to_Msun", [-1.0])[0],
-        particle_masses=f("particle_masses"), flux_model=FLUX_LAWS[case["flux_law"]])
+        particle_masses=f("particle_masses"), flux_model=FLUX_LAWS[case["flux_law"]],
+        halos=(tuple(case["halos"][:, k] for k in range(4)) if len(case["halos"]) else None))

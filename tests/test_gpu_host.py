@@ -62,10 +62,15 @@ def test_cpp_example_program_renders(tmp_path):
 
 
 @pytest.mark.parametrize("name", ["flux_ann_somv_ns32", "flux_ann_somv2_ns32", "flux_ann_pwave_ns32",
-                                  "flux_decay_ns32", "flux_ann_adiabatic_ns16"])
+                                  "flux_decay_ns32", "flux_ann_adiabatic_ns16", "flux_ann_core_nosom_ns16"])
 def test_cpp_genmap_flux_laws(tmp_path, name):
     import golden_cases as G
+    from annmap.halocore import write_halo_table
     case, info = write_case(tmp_path, name, mem_buffer=250)
-    mp, total = host.genmap(info, COMP, flux_model=G.FLUX_LAWS[case["flux_law"]])
+    hfile = ""
+    if len(case["halos"]):
+        hfile = str(tmp_path / "halos.data")
+        write_halo_table(hfile, *[case["halos"][:, k] for k in range(4)])
+    mp, total = host.genmap(info, COMP, flux_model=G.FLUX_LAWS[case["flux_law"]], halo_file=hfile)
     par = annmap.Parameters(info)
     check(mp, case["map"], COMP, total=case["map"].sum() * par.map.dOmega, dOmega=par.map.dOmega)

@@ -65,6 +65,8 @@ def test_golden_maps(rend, name, precision):
     case = G.load(name)
     p = annmap.Parameters(text=case["info_text"].replace("@DIR@", "/x"))
     rend.set_params(p, flux_model=case["flux_law"])
+    if len(case["halos"]):
+        rend.set_halo_cores(*[case["halos"][:, k] for k in range(4)])
     got = rend.render(case["parts"], p.map.Nside, precision)
     ref = case["map"]
     st = rend.stats()

@@ -117,3 +117,17 @@ def test_cpp_example_program_reads_like_the_reference(tmp_path):
     assert d["masked"] == int((parts["rho"] < 0).sum())
     assert d["chunks"] == -(-len(parts["x"]) // 333)
     assert d["mass_sum"] == pytest.approx(float(np.sum(parts["m"].astype(np.float64))), rel=1e-12)
+
+
+def test_halo_table_roundtrip(tmp_path):
+    from annmap.halocore import read_halo_table, write_halo_table
+    rng = np.random.default_rng(4)
+    h = [rng.normal(size=50).astype(np.float32) for _ in range(4)]
+    p = str(tmp_path / "h.data")
+    write_halo_table(p, *h)
+    got = read_halo_table(p)
+    for a, b in zip(got, h):
+        assert np.array_equal(a, b)
+    (tmp_path / "e.data").write_text("")
+    with pytest.raises(ValueError):
+        read_halo_table(str(tmp_path / "e.data"))
