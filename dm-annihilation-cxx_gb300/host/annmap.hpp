@@ -113,6 +113,15 @@ public:
     // Native file (int32 count, then 48-byte records); optional byte mask
     // file (int32 count, one byte per particle; 0 masks: dens = -1).
     DataReader(const std::string &path, bool isMask = false, const std::string &maskfile = "");
+    // Tipsy XDR particle file (big-endian: header time, nbodies, ndim, nsph,
+    // ndark, nstar, pad; then gas, dark and star records -- only the dark
+    // ones are read, src/datareader.cpp:120-190) with the density, smoothing
+    // length and velocity dispersion side files of "smooth" (native int32
+    // count of all bodies, then one float per body, gas first).  With
+    // isSingleFile the side files are not read and those fields are 0.
+    DataReader(const std::string &partfile, const std::string &densfile,
+               const std::string &hsmoothfile, const std::string &sigmafile, bool isMask = false,
+               const std::string &maskfile = "", bool isSingleFile = false);
     ~DataReader();
     DataReader(const DataReader &) = delete;
     DataReader &operator=(const DataReader &) = delete;
@@ -133,7 +142,11 @@ public:
 
 private:
     std::string path_, maskPath_;
+    std::string densPath_, hsmPath_, sigmaPath_;
     bool isMask_;
+    bool isNative_ = true, isSingleFile_ = false;
+    void *dfp_ = nullptr, *hfp_ = nullptr, *sfp_ = nullptr;   // FILE * of the side files
+    std::vector<unsigned char> raw_;
     bool open_ = false;
     void *fp_ = nullptr, *mfp_ = nullptr;    // FILE *
     unsigned int partNumbers_ = 0;

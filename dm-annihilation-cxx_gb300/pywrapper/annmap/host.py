@@ -25,6 +25,9 @@ def load():
         L.annmap_read_native.argtypes = [C.c_char_p, C.c_char_p, C.c_int, C.c_int,
                                          C.POINTER(C.c_float), C.c_int64, C.c_char_p, C.c_int]
         L.annmap_read_native.restype = C.c_int64
+        L.annmap_read_tipsy.argtypes = [C.c_char_p] * 5 + [C.c_int, C.c_int, C.c_int,
+                                                           C.POINTER(C.c_float), C.c_int64, C.c_char_p, C.c_int]
+        L.annmap_read_tipsy.restype = C.c_int64
         L.annmap_genmap.argtypes = [C.c_char_p, C.c_int, C.c_int, C.c_int, C.c_char_p, D, C.c_int64, D,
                                     C.c_char_p, C.c_int]
         L.annmap_genmap.restype = C.c_int
@@ -39,27 +42,43 @@ def _err():
 
 
 def parse_info(path: str) -> dict:
-    out = (C.c_double * 23)()
+    out = (C.c_double * 24)()
     e = _err()
     if load().annmap_parse_info(path.encode(), out, e, 512) != 0:
         raise ValueError(e.value.decode())
     v = out[:]
     return {"nside": int(v[0]), "rotmatrix": np.array(v[1:10]).reshape(3, 3), "opos": v[10:13],
             "cpos": v[13:16], "unit_factor": v[16], "hires_threshold": v[17], "memParts": int(v[18]),
-            "testNum": int(v[19]), "otheta": v[20], "ophi": v[21], "isMask": bool(v[22])}
+            "testNum": int(v[19]), "otheta": v[20], "ophi": v[21], "isMask": bool(v[22]),
+            "isNative": bool(v[23])}
+
+
+SOA = ("x", "y", "z", "m", "rho", "h", "sigmav")
 
 
 def read_native(path: str, maskfile: str = "", test: int = -1, buf: int = 10000000, cap: int = None) -> dict:
     if cap is None:
         with open(path, "rb") as f:
             cap = max(1, int(np.fromfile(f, dtype="<i4", count=1)[0]))
-    soa = np.zeros((6, cap), dtype=np.float32)
+    soa = np.zeros((7, cap), dtype=np.float32)
     e = _err()
     n = load().annmap_read_native(path.encode(), maskfile.encode(), int(test), int(buf),
                                   soa.ctypes.data_as(C.POINTER(C.c_float)), cap, e, 512)
     if n < 0:
         raise ValueError(e.value.decode())
-    return {k: soa[i, :n].copy() for i, k in enumerate(("x", "y", "z", "m", "rho", "h"))}
+    return {k: soa[i, :n].copy() for i, k in enumerate(SOA)}
+
+
+def read_tipsy(part: str, dens: str, hsm: str, sigv: str, maskfile: str = "", single: bool = False,
+               test: int = -1, buf: int = 10000000, cap: int = 1 << 20) -> dict:
+    soa = np.zeros((7, cap), dtype=np.float32)
+    e = _err()
+    n = load().annmap_read_tipsy(part.encode(), dens.encode(), hsm.encode(), sigv.encode(),
+                                 maskfile.encode(), int(single), int(test), int(buf),
+                                 soa.ctypes.data_as(C.POINTER(C.c_float)), cap, e, 512)
+    if n < 0:
+        raise ValueError(e.value.decode())
+    return {k: soa[i, :n].copy() for i, k in enumerate(SOA)}
 
 
 def genmap(info_file: str, precision: int = 1, device: int = 0, nside: int = None,

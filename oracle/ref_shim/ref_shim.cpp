@@ -10,8 +10,8 @@
  *   - MapGenerator's constructor/destructor/accessors: the reference defines
  *     them in src/mapgenerator.cpp:18-74 next to saveToFits(), which needs
  *     HEALPix FITS I/O; they are restated here with the same behaviour.
- *   - XDR / Tipsy entry points (src/tipsy_io.c, <rpc/xdr.h>): stubs that fail,
- *     because only the native particle format is exercised.
+ *   - XDR / Tipsy entry points (src/tipsy_io.c, <rpc/xdr.h>): the decode
+ *     side the reference's DataReader calls, reading big-endian values.
  *
  * Usage: annmap_ref <info.ini> <map.bin> <params.txt>
  *   writes Npix doubles (the map after the dOmega division) to map.bin and
@@ -28,11 +28,49 @@
 #include "mapgenerator.h"
 
 extern "C" {
-void xdrstdio_create(XDR *, FILE *, enum xdr_op) {}
-void xdr_destroy(XDR *) {}
+void xdrstdio_create(XDR *x, FILE *f, enum xdr_op op) {
+    x->x_op = op;
+    x->fp = f;
 }
-int xdr_header(XDR *, tipsy_header *) { return 0; }
-int xdr_dark(XDR *, struct dark_particle *) { return 0; }
+void xdr_destroy(XDR *x) { x->fp = NULL; }
+}
+
+// XDR decoding of the Tipsy header and dark records (the layout of
+// src/tipsy_io.c:159-192's xdr_header / xdr_dark): big-endian 4-byte ints and
+// floats, 8-byte double.
+static bool xdr_u32(XDR *x, unsigned int *v) {
+    unsigned char b[4];
+    if (fread(b, 1, 4, x->fp) != 4) return false;
+    *v = ((unsigned int)b[0] << 24) | ((unsigned int)b[1] << 16) | ((unsigned int)b[2] << 8) | b[3];
+    return true;
+}
+static bool xdr_f32(XDR *x, float *v) {
+    unsigned int u;
+    if (!xdr_u32(x, &u)) return false;
+    memcpy(v, &u, 4);
+    return true;
+}
+int xdr_header(XDR *x, tipsy_header *h) {
+    unsigned int hi, lo, v[6];
+    if (!xdr_u32(x, &hi) || !xdr_u32(x, &lo)) return 0;
+    unsigned long long u = ((unsigned long long)hi << 32) | lo;
+    memcpy(&h->time, &u, 8);
+    for (int k = 0; k < 6; k++)
+        if (!xdr_u32(x, &v[k])) return 0;
+    h->nbodies = (int)v[0];
+    h->ndim = (int)v[1];
+    h->nsph = (int)v[2];
+    h->ndark = (int)v[3];
+    h->nstar = (int)v[4];
+    return 1;
+}
+int xdr_dark(XDR *x, struct dark_particle *p) {
+    float *f[9] = {&p->mass, &p->pos[0], &p->pos[1], &p->pos[2], &p->vel[0], &p->vel[1], &p->vel[2],
+                   &p->eps, &p->phi};
+    for (int k = 0; k < 9; k++)
+        if (!xdr_f32(x, f[k])) return 0;
+    return 1;
+}
 
 MapGenerator::MapGenerator(Parameters *par, DataReader *reader) {
     par_ = par;
@@ -53,7 +91,12 @@ int main(int argc, char **argv) {
         return 2;
     }
     Parameters par(argv[1]);
-    DataReader *reader = new DataReader(par.nativeDatafile, par.isMask, par.maskFileName);
+    DataReader *reader;
+    if (par.isNative)
+        reader = new DataReader(par.nativeDatafile, par.isMask, par.maskFileName);
+    else   // src/main.cpp:46-53
+        reader = new DataReader(par.partFile, par.densFile, par.hsmFile, par.dspFile, par.isMask,
+                                par.maskFileName);
     reader->setTest(par.testNum);
     reader->setBuf(par.memParts);
     reader->open();

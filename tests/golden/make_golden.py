@@ -51,6 +51,42 @@ def write_native(path, P, extra_mass=None, sigmav=None):
     return rec
 
 
+def write_tipsy(d, P, rng):
+    """The reference's XDR input (src/datareader.cpp:120-190, src/tipsy_io.c):
+    a big-endian Tipsy file with 7 gas, the dark particles of P and 3 star
+    particles, and the density / hsmooth / sigmav side files of "smooth"
+    (native int32 count of all bodies, then one float per body, gas first).
+    Returns the DMParticle records of the dark particles."""
+    nsph, ndark, nstar = 7, len(P), 3
+    nb = nsph + ndark + nstar
+    dark = np.zeros((ndark, 9), np.float32)
+    dark[:, 0] = P.m
+    dark[:, 1], dark[:, 2], dark[:, 3] = P.x, P.y, P.z
+    dark[:, 4:7] = rng.normal(0, 100, (ndark, 3))
+    dark[:, 7] = 0.01
+    dark[:, 8] = rng.normal(0, 1, ndark)
+    paths = {k: os.path.join(d, k + ".bin") for k in ("tipsy", "dens", "hsm", "sigv")}
+    with open(paths["tipsy"], "wb") as f:
+        f.write(np.array([0.5], ">f8").tobytes())
+        f.write(np.array([nb, 3, nsph, ndark, nstar, 0], ">i4").tobytes())
+        f.write(rng.normal(size=(nsph, 12)).astype(">f4").tobytes())
+        f.write(dark.astype(">f4").tobytes())
+        f.write(rng.normal(size=(nstar, 11)).astype(">f4").tobytes())
+    sv = rng.lognormal(np.log(3000.0), 1.0, ndark).astype(np.float32)
+    side = {"dens": P.rho, "hsm": P.h, "sigv": sv}
+    for k, v in side.items():
+        with open(paths[k], "wb") as f:
+            np.array([nb], np.int32).tofile(f)
+            np.concatenate([rng.uniform(1, 2, nsph), v, rng.uniform(1, 2, nstar)]).astype(np.float32).tofile(f)
+    rec = np.zeros((ndark, 12), np.float32)
+    rec[:, 0], rec[:, 1], rec[:, 2] = P.m, P.rho, P.h
+    rec[:, 3:6] = dark[:, 1:4]
+    rec[:, 6:9] = dark[:, 4:7]
+    rec[:, 9], rec[:, 10], rec[:, 11] = sv, dark[:, 7], dark[:, 8]
+    files = {k: np.frombuffer(open(p_, "rb").read(), np.uint8) for k, p_ in paths.items()}
+    return rec, paths, files
+
+
 def parse_params(text):
     out = {}
     for line in text.strip().splitlines():
@@ -61,14 +97,18 @@ def parse_params(text):
 
 def run_case(name, P, *, nside, info_extra="", mass=None, mask=None, particle_masses=None,
              obs=None, centre=(0.0, 0.0, 0.0), align=(0.0, 0.0, 1.0), units="kpc",
-             mem_buffer=1000, test=None, law="ann_nosom", sigmav=None, halos=None):
+             mem_buffer=1000, test=None, law="ann_nosom", sigmav=None, halos=None, tipsy=False):
     d = tempfile.mkdtemp(prefix="golden_")
     if halos is not None:   # the core law reads ./halocore/VL2_Halos.data (x y z radius lines)
         os.makedirs(os.path.join(d, "halocore"))
         with open(os.path.join(d, "halocore", "VL2_Halos.data"), "w") as f:
             for row in np.stack(halos, axis=1):
                 f.write("\t".join(repr(float(np.float32(v))) for v in row) + "\n")
-    rec = write_native(os.path.join(d, "parts.bin"), P, extra_mass=mass, sigmav=sigmav)
+    tipsy_files = {}
+    if tipsy:
+        rec, tpaths, tipsy_files = write_tipsy(d, P, np.random.Generator(np.random.PCG64(1113)))
+    else:
+        rec = write_native(os.path.join(d, "parts.bin"), P, extra_mass=mass, sigmav=sigmav)
     obs = P.obs_pos if obs is None else obs
     pm = particle_masses if particle_masses is not None else [P.particle_mass]
     lines = ["# golden case " + name, "Omega_M = 0.238", "h100 = 0.73", "n_s = 0.951",
@@ -81,8 +121,12 @@ def run_case(name, P, *, nside, info_extra="", mass=None, mask=None, particle_ma
               "centerpos = " + " ".join(repr(float(x)) for x in centre),
               "align_vec = " + " ".join(repr(float(x)) for x in align),
               "obs_pos = " + " ".join(repr(float(x)) for x in obs),
-              f"nside = {nside}", f"mem_buffer = {mem_buffer}",
-              f"datafile = {d}/parts.bin"]
+              f"nside = {nside}", f"mem_buffer = {mem_buffer}"]
+    if tipsy:
+        lines += [f"partfile = {d}/tipsy.bin", f"densfile = {d}/dens.bin", f"hsmfile = {d}/hsm.bin",
+                  f"vdspfile = {d}/sigv.bin"]
+    else:
+        lines += [f"datafile = {d}/parts.bin"]
     if test is not None:
         lines.append(f"test = {test}")
     if mask is not None:
@@ -105,7 +149,7 @@ def run_case(name, P, *, nside, info_extra="", mass=None, mask=None, particle_ma
     np.savez_compressed(
         os.path.join(HERE, name + ".npz"), map=mp, info=np.array(ini.replace(d, "@DIR@")),
         records=rec, mask=(np.asarray(mask, np.uint8) if mask is not None else np.zeros(0, np.uint8)),
-        flux_law=np.array(law),
+        flux_law=np.array(law), **{"tipsy_" + k: v for k, v in tipsy_files.items()},
         halos=(np.stack(halos, axis=1).astype(np.float32) if halos is not None else np.zeros((0, 4), np.float32)),
         **{"par_" + k: v for k, v in par.items()})
     assert np.all(np.isfinite(mp)), name
@@ -186,6 +230,11 @@ def main():
     run_case("flux_ann_core_nosom_ns16", R, nside=16, units="vl2", particle_masses=[4.1e-9],
              obs=obs, centre=tuple(c.tolist()), align=(-0.025836, 0.133297, 0.990739),
              law="ann_core_nosom", halos=halos)
+    # 9. the Tipsy XDR input (gas and star particles skipped, side files of
+    #    "smooth"), chunked and with a mask, under the somv law (reads sigmav)
+    P = synth.nfw_halo(1100, seed=112, n_sub=2)
+    mask = (np.random.Generator(np.random.PCG64(1114)).uniform(size=len(P)) > 0.1).astype(np.uint8)
+    run_case("tipsy_somv_ns32", P, nside=32, tipsy=True, mask=mask, mem_buffer=300, law="ann_somv")
 
 
 if __name__ == "__main__":

@@ -15,12 +15,17 @@ def write_case(tmp_path, name="hires_mask_ns32", mem_buffer=333, output=None):
     with open(data, "wb") as f:
         np.array([len(rec)], np.int32).tofile(f)
         rec.tofile(f)
+    for k in ("tipsy", "dens", "hsm", "sigv"):   # a Tipsy case's XDR input and side files
+        if "tipsy_" + k in z.files:
+            with open(os.path.join(str(tmp_path), k + ".bin"), "wb") as f:
+                f.write(z["tipsy_" + k].tobytes())
     mpath = os.path.join(str(tmp_path), "mask.bin")
     if mask.size:
         with open(mpath, "wb") as f:
             np.array([len(rec)], np.int32).tofile(f)
             mask.tofile(f)
     text = case["info_text"].replace("@DIR@/parts.bin", data).replace("@DIR@/mask.bin", mpath)
+    text = text.replace("@DIR@", str(tmp_path))
     lines = [ln for ln in text.split("\n") if not ln.startswith("mem_buffer") and not ln.startswith("outputmap")]
     lines.append(f"mem_buffer = {mem_buffer}")
     if output:

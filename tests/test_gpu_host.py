@@ -74,3 +74,22 @@ def test_cpp_genmap_flux_laws(tmp_path, name):
     mp, total = host.genmap(info, COMP, flux_model=G.FLUX_LAWS[case["flux_law"]], halo_file=hfile)
     par = annmap.Parameters(info)
     check(mp, case["map"], COMP, total=case["map"].sum() * par.map.dOmega, dOmega=par.map.dOmega)
+
+
+@pytest.mark.parametrize("precision", [PLAIN, COMP])
+def test_cpp_and_python_tipsy_input_match_golden(tmp_path, precision):
+    """The Tipsy XDR input (through the reference's own XDR reader for the
+    golden map) via the C++ and the Python MapGenerator, somv law."""
+    case, info = write_case(tmp_path, "tipsy_somv_ns32", mem_buffer=300)
+    par = annmap.Parameters(info)
+    assert not par.isNative
+    mp, total = host.genmap(info, precision, flux_model=annmap._lib.FLUX_ANN_SOMV)
+    check(mp, case["map"], precision)
+    reader = annmap.DataReader.tipsy(par.partFile, par.densFile, par.hsmFile, par.dspFile,
+                                     par.isMask, par.maskFileName)
+    reader.setTest(par.testNum)
+    reader.setBuf(par.memParts)
+    reader.open()
+    gen = annmap.MapGenerator(par, reader, precision=precision, flux_model="ann_somv")
+    gen.start()
+    check(gen.getMap(), case["map"], precision)

@@ -131,3 +131,30 @@ def test_halo_table_roundtrip(tmp_path):
     (tmp_path / "e.data").write_text("")
     with pytest.raises(ValueError):
         read_halo_table(str(tmp_path / "e.data"))
+
+
+@pytest.mark.parametrize("buf,test", [(10000000, -1), (300, -1), (128, 1000)])
+def test_tipsy_readers_match_the_reference_records(tmp_path, buf, test):
+    """The Tipsy XDR input of the golden case (made through the reference's own
+    XDR reader) through the C++ and the Python DataReader."""
+    case, info = write_case(tmp_path, "tipsy_somv_ns32")
+    d = str(tmp_path)
+    files = [os.path.join(d, k + ".bin") for k in ("tipsy", "dens", "hsm", "sigv")]
+    got = host.read_tipsy(*files, maskfile=os.path.join(d, "mask.bin"), test=test, buf=buf)
+    r = DataReader.tipsy(*files, isMask=True, maskfile=os.path.join(d, "mask.bin"))
+    r.setBuf(buf)
+    r.setTest(test)
+    r.open()
+    py = {k: [] for k in got}
+    while r.hasNext():
+        c = r.next_chunk()
+        for k in py:
+            py[k].append(c[k])
+    n = len(case["parts"]["x"]) if test == -1 else test
+    for k in got:
+        exp = case["parts"][k][:n]
+        assert np.array_equal(got[k], exp), k
+        assert np.array_equal(np.concatenate(py[k]), exp), k
+    single = host.read_tipsy(*files, single=True, buf=buf)
+    assert np.all(single["rho"] == 0) and np.array_equal(single["x"], case["parts"]["x"])
+    assert host.parse_info(info)["isNative"] is False
