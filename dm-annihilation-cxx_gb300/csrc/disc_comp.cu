@@ -27,12 +27,15 @@
 // instructions of sm_100+ (__ffma2_rn & co.), halving the issue slots of the
 // polynomial, Kahan and TwoSum arithmetic.
 //
-// Polynomials (written from their Taylor series):
-//   sin x = x - x^3/3! + x^5/5! - ... ; to x^7 for |x| < 0.35 (error
-//   < 3e-10 relative), to x^15 for |x| <= pi/2 (error < 1e-11);
+// Polynomials (written from their Taylor series), the number of terms chosen
+// per particle from the largest |x| and h its disc can reach:
+//   sin x = x - x^3/3! + x^5/5! - ... ; to x^3 for |x| < 0.025 (error
+//   < 3.3e-9 relative), to x^7 for |x| < 0.35 (< 3e-10), to x^15 for
+//   |x| <= pi/2 (< 1e-11);
 //   asin^2(sqrt h) = sum_n (4h)^n / (2 n^2 C(2n,n)) = h + h^2/3 + 8h^3/45 +
-//   4h^4/35 + 128h^5/1575 + ... ; five terms for h < 0.02 (error < 3e-10
-//   relative); otherwise asinf(sqrtf(h)) from the CUDA math library.
+//   4h^4/35 + 128h^5/1575 + ... ; three terms for h < 4e-3 (error < 7.4e-9
+//   relative), five for h < 0.02 (< 3e-10); otherwise asinf(sqrtf(h)) from
+//   the CUDA math library.  All truncation errors stay below FP32 rounding.
 #include "kernels.cuh"
 
 namespace dmann {
@@ -69,7 +72,7 @@ struct alignas(16) Run {
 
 struct Ext {
     float nK;           // -K
-    int small_h, small_x;
+    int tier_h, tier_x;  // polynomial lengths (0 shortest, 2 general)
 };
 
 // Per-particle constants of the FP32 chord test (see chord_fast).
@@ -99,7 +102,7 @@ __device__ inline void particle_setup(const Hpx &g, const DiscHdr &d, Ext &e, Ch
         const double s = sin(0.5 * d.R);
         hmax = s * s;
     }
-    e.small_h = hmax < 0.02;
+    e.tier_h = hmax < 4e-3 ? 0 : hmax < 0.02 ? 1 : 2;
     ch.hR = (float)hmax;
     ch.sth0 = (float)d.sth0;
     ch.fast = !d.allsky && d.sth0 > 1e-3;
@@ -111,12 +114,15 @@ __device__ inline void particle_setup(const Hpx &g, const DiscHdr &d, Ext &e, Ch
         ch.cf[k] = (float)(c - fl);
     }
     const bool caps = d.allsky || d.r_first < d.irmin || d.r_last > d.irmax;
-    int small_x = 0;
+    int tier_x = 2;
     if (!caps) {
         const double sr = sin(d.R);
-        if (sr < 0.999 * d.sth0) small_x = (0.5 * asin(sr / d.sth0)) < 0.33;
+        if (sr < 0.999 * d.sth0) {
+            const double xm = 0.5 * asin(sr / d.sth0);   // largest half azimuth offset
+            tier_x = xm < 0.025 ? 0 : xm < 0.33 ? 1 : 2;
+        }
     }
-    e.small_x = small_x;
+    e.tier_x = tier_x;
 }
 
 __device__ inline bool near_int_f(float a, float tau) {
@@ -278,7 +284,9 @@ __device__ __forceinline__ float2 weight2(const Ext &e, const Run &r, float2 jj)
     const float2 x = fma2(jj, f2(r.steph), f2(r.d0h));
     const float2 x2 = mul2(x, x);
     float2 p;
-    if (e.small_x) {
+    if (e.tier_x == 0) {
+        p = fma2(x2, f2(-1.0f / 6.0f), f2(1.0f));
+    } else if (e.tier_x == 1) {
         p = fma2(x2, f2(-1.0f / 5040.0f), f2(1.0f / 120.0f));
         p = fma2(x2, p, f2(-1.0f / 6.0f));
         p = fma2(x2, p, f2(1.0f));
@@ -294,7 +302,11 @@ __device__ __forceinline__ float2 weight2(const Ext &e, const Run &r, float2 jj)
     const float2 sn = mul2(x, p);
     const float2 h = fma2(f2(r.B), mul2(sn, sn), f2(r.A));
     float2 g;
-    if (e.small_h) {
+    if (e.tier_h == 0) {
+        float2 q = fma2(h, f2(8.0f / 45.0f), f2(1.0f / 3.0f));
+        q = fma2(h, q, f2(1.0f));
+        g = mul2(h, q);
+    } else if (e.tier_h == 1) {
         float2 q = fma2(h, f2(128.0f / 1575.0f), f2(4.0f / 35.0f));
         q = fma2(h, q, f2(8.0f / 45.0f));
         q = fma2(h, q, f2(1.0f / 3.0f));
@@ -323,7 +335,7 @@ template <int G, int RCH>
 __device__ inline int build_runs(const DiscArgs &a, CompSmem<RCH> &sm, int r0, int n) {
     using Gp = Grp<G>;
     int c = 0;
-    const bool need_a2 = !sm.ext.small_h;
+    const bool need_a2 = sm.ext.tier_h == 2;
     for (int i = Gp::rank(); i < n; i += G) c += make_runs(a, sm.hdr, sm.ch, need_a2, r0 + i, &sm.run[2 * i]);
     c = __reduce_add_sync(0xffffffffu, c);
     if (G > 32) {
