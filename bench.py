@@ -453,6 +453,16 @@ def bench_adjoint(dev):
     r.adjoint(dparts, nside, G, out=out)
     dt = time.perf_counter() - t0
     st = r.stats()
+    # the compensated-FP32 adjoint of the same loss, and its distance to the FP64 one
+    out_c = torch.empty_like(out)
+    r.adjoint(dparts, nside, G, out=out_c, precision=annmap.COMP_F32)
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    r.adjoint(dparts, nside, G, out=out_c, precision=annmap.COMP_F32)
+    dtc = time.perf_counter() - t1
+    stc = r.stats()
+    rel = [float(torch.linalg.vector_norm(out_c[k] - out[k]) / torch.linalg.vector_norm(out[k]))
+           for k in range(6)]
     fwd = torch.empty(12 * nside * nside, dtype=torch.float64, device=dev)
     r.render(dparts, nside, annmap.PLAIN_F64, out=fwd)
     fst = r.stats()
@@ -460,7 +470,9 @@ def bench_adjoint(dev):
     return {"workload": "nfw4m_sub20_adjoint", "particles": len(P), "nside": nside,
             "ms": dt * 1e3, "kernel_ms": st["kernel_ms"], "particles_per_s": len(P) / dt,
             "deposits": st["deposits"], "plain_forward_kernel_ms": fst["kernel_ms"],
-            "form": "FP64 adjoint of the plain form (two passes per disc)"}
+            "form": "FP64 adjoint of the plain form (two passes per disc)",
+            "comp_f32": {"ms": dtc * 1e3, "kernel_ms": stc["kernel_ms"], "particles_per_s": len(P) / dtc,
+                         "normwise_rel_diff_vs_fp64": dict(zip(["x", "y", "z", "m", "rho", "h"], rel))}}
 
 
 def main():

@@ -1,0 +1,97 @@
+// adjoint_common.cuh -- the per-particle epilogue shared by the FP64 adjoint
+// (adjoint.cu) and the compensated-FP32 adjoint (disc_comp.cu): given a
+// particle's Gb = dL/dF, K T and K V (see adjoint.cu for the formulas), the
+// gradient with respect to x, y, z, m, rho, h and its observer terms.
+#pragma once
+#include "kernels.cuh"
+
+namespace dmann {
+namespace adj {
+
+constexpr double kInvC2 = 1.0 / 0.333;  // 2 c
+
+struct AdjArgs {
+    DiscArgs d;                 // geometry from the prep kernel, queue, counters
+    Particles p;
+    const signed char *cls;     // PClass per particle
+    const double *gmap;         // dL/dmap [npix]
+    const float *gmap32;        // the same rounded to FP32 (the compensated adjoint)
+    double inv_dOmega;
+    double *grad;               // [6][n]: x, y, z, m, rho, h
+    double *oacc;               // [12]: sum_i dL/du_i (3), dL/dR row-major (9)
+};
+
+// u = pos - opos and d exactly as the prep kernel forms them.
+__device__ inline double particle_u(const AdjArgs &a, int i, double u[3]) {
+    u[0] = (double)a.p.x[i] - a.d.f.opos[0];
+    u[1] = (double)a.p.y[i] - a.d.f.opos[1];
+    u[2] = (double)a.p.z[i] - a.d.f.opos[2];
+    return sqrt(u[0] * u[0] + u[1] * u[1] + u[2] * u[2]);
+}
+
+// Writes particle i's gradient and adds its observer terms to acc.
+// Gb = dL/dF; KT = K T and KV = K V (zero for a single-pixel deposit).
+__device__ inline void write_grad(const AdjArgs &a, int i, double Gb, double KT,
+                                  const double KV[3], bool disc, double acc[12]) {
+    double u[3];
+    const double d = particle_u(a, i, u);
+    const double inv_d = 1.0 / d;
+    const double uh[3] = {u[0] * inv_d, u[1] * inv_d, u[2] * inv_d};
+    const double m = (double)a.p.m[i], rho = (double)a.p.rho[i];
+    const double fd = a.d.f.unit_factor / (4.0 * kPi * d * d);   // F / (rho m)
+    const double F = fd * rho * m;
+    const double w[3] = {-KV[0], -KV[1], KV[2]};                 // D K V
+    const double cr = -(2.0 * Gb * F + KT) * inv_d;
+    const int n = a.p.n;
+#pragma unroll
+    for (int j = 0; j < 3; j++) {
+        const double rw = a.d.f.rot[j][0] * w[0] + a.d.f.rot[j][1] * w[1] + a.d.f.rot[j][2] * w[2];
+        const double g = cr * uh[j] + rw * inv_d;
+        a.grad[(size_t)j * n + i] = g;
+        acc[j] += g;
+    }
+    a.grad[(size_t)3 * n + i] = Gb * fd * rho;
+    a.grad[(size_t)4 * n + i] = Gb * fd * m;
+    a.grad[(size_t)5 * n + i] = disc ? KT / (double)a.p.h[i] : 0.0;
+    if (disc) {
+#pragma unroll
+        for (int j = 0; j < 3; j++)
+#pragma unroll
+            for (int k = 0; k < 3; k++) acc[3 + 3 * j + k] += uh[j] * w[k];
+    }
+}
+
+// Sum of NV values over a group (one warp, or a block of G threads);
+// every thread of the group gets the sums.
+template <int G, int NV>
+__device__ inline void group_sum(double v[NV], double (*red)[32]) {
+#pragma unroll
+    for (int k = 0; k < NV; k++) v[k] = warp_sum(v[k]);
+    if (G > 32) {
+        const int r = threadIdx.x;
+        if ((r & 31) == 0)
+#pragma unroll
+            for (int k = 0; k < NV; k++) red[k][r >> 5] = v[k];
+        __syncthreads();
+#pragma unroll
+        for (int k = 0; k < NV; k++) {
+            double s = 0.0;
+            for (int w = 0; w < G / 32; w++) s += red[k][w];
+            v[k] = s;
+        }
+        __syncthreads();
+    }
+}
+
+__device__ inline void flush_acc(double *oacc, const double acc[12]) {
+#pragma unroll
+    for (int k = 0; k < 12; k++)
+        if (acc[k] != 0.0) atomicAdd(oacc + k, acc[k]);
+}
+
+}  // namespace adj
+
+// disc_comp.cu: the compensated-FP32 adjoint's disc kernels
+cudaError_t launch_adjoint_comp_discs(const adj::AdjArgs &a, int num_sms, cudaStream_t s);
+
+}  // namespace dmann

@@ -896,8 +896,11 @@ dmann_status dmann_render_batch(dmann_ctx *ctx, const float *x, const float *y, 
 
 dmann_status dmann_adjoint(dmann_ctx *ctx, const float *x, const float *y, const float *z,
                            const float *m, const float *rho, const float *h, int64_t n, int nside,
-                           const double *grad_map, double *grad, double grad_opos[3]) {
+                           int precision, const double *grad_map, double *grad,
+                           double grad_opos[3]) {
     if (!ctx) return DMANN_ERR_INVALID;
+    if (precision != DMANN_PLAIN_F64 && precision != DMANN_COMP_F32)
+        return fail(ctx, DMANN_ERR_INVALID, "unknown precision form");
     if (!grad_map || !grad || !grad_opos)
         return fail(ctx, DMANN_ERR_INVALID, "grad_map, grad and grad_opos are required");
     if (nside < 1 || nside > 8192) return fail(ctx, DMANN_ERR_INVALID, "nside must be in [1, 8192]");
@@ -921,6 +924,7 @@ dmann_status dmann_adjoint(dmann_ctx *ctx, const float *x, const float *y, const
         (st = ensure(ctx, ctx->hist, 4 * (size_t)kKeys)) || (st = ensure(ctx, ctx->ctr, 8 * C_COUNT)) ||
         (st = ensure(ctx, ctx->fsum, 8)) || (st = ensure(ctx, ctx->oacc, 8 * 12)))
         return st;
+    if (precision == DMANN_COMP_F32 && (st = ensure(ctx, ctx->acc, 4 * P)) != DMANN_OK) return st;
     const float *src[6] = {x, y, z, m, rho, h};
     const float *dev[6];
     for (int k = 0; k < 6; k++) {
@@ -983,7 +987,8 @@ dmann_status dmann_adjoint(dmann_ctx *ctx, const float *x, const float *y, const
     da.ctr = pa.ctr;
     da.acc = pa.acc;
     CK(cudaEventRecord(ctx->evd0, s));
-    CK(launch_adjoint(da, pa.p, pa.out.cls, dgmap, dgrad, (double *)ctx->oacc.p, ctx->num_sms, s));
+    CK(launch_adjoint(da, pa.p, pa.out.cls, dgmap, (float *)ctx->acc.p, dgrad, (double *)ctx->oacc.p,
+                      precision, ctx->num_sms, s));
     CK(cudaEventRecord(ctx->evd1, s));
     CK(cudaEventRecord(ctx->evdm, s));
     CK(cudaEventRecord(ctx->ev1, s));

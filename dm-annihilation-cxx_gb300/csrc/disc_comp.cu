@@ -36,6 +36,7 @@
 //   4h^4/35 + 128h^5/1575 + ... ; three terms for h < 4e-3 (error < 7.4e-9
 //   relative), five for h < 0.02 (< 3e-10); otherwise asinf(sqrtf(h)) from
 //   the CUDA math library.  All truncation errors stay below FP32 rounding.
+#include "adjoint_common.cuh"
 #include "kernels.cuh"
 
 namespace dmann {
@@ -279,8 +280,10 @@ __device__ inline float g_general(float h, float x, const Run &r) {
     return t * t;
 }
 
-// Weights of pixels jj = (j, j + 32) of run r.
-__device__ __forceinline__ float2 weight2(const Ext &e, const Run &r, float2 jj) {
+// Weights of pixels jj = (j, j + 32) of run r; also sin(x) (x half the
+// azimuth offset), the haversine h of the distance and g = theta^2 / 4.
+__device__ __forceinline__ float2 weight2x(const Ext &e, const Run &r, float2 jj, float2 &sn_out,
+                                          float2 &h_out, float2 &g_out) {
     const float2 x = fma2(jj, f2(r.steph), f2(r.d0h));
     const float2 x2 = mul2(x, x);
     float2 p;
@@ -316,7 +319,15 @@ __device__ __forceinline__ float2 weight2(const Ext &e, const Run &r, float2 jj)
         g = make_float2(g_general(h.x, x.x, r), g_general(h.y, x.y, r));
     }
     const float2 t = mul2(g, f2(e.nK));
+    sn_out = sn;
+    h_out = h;
+    g_out = g;
     return make_float2(ex2_approx(t.x), ex2_approx(t.y));
+}
+
+__device__ __forceinline__ float2 weight2(const Ext &e, const Run &r, float2 jj) {
+    float2 sn, h, g;
+    return weight2x(e, r, jj, sn, h, g);
 }
 
 template <int G>
@@ -331,12 +342,28 @@ struct Grp {
 
 // Stages rings r0 .. r0+n-1 as runs; returns the chunk's pixel count (all
 // threads of the group).
+// Per-ring terms of the adjoint's tangent vector (see adjc_particle).
+struct AdjRing {
+    float sr;    // sin(theta_r - theta0)
+    float cr;    // 2 cos(theta0) sin(theta_r)
+    float st2;   // 2 sin(theta_r)
+};
+
 template <int G, int RCH>
-__device__ inline int build_runs(const DiscArgs &a, CompSmem<RCH> &sm, int r0, int n) {
+__device__ inline int build_runs(const DiscArgs &a, CompSmem<RCH> &sm, int r0, int n,
+                                 AdjRing *aring = nullptr) {
     using Gp = Grp<G>;
     int c = 0;
     const bool need_a2 = sm.ext.tier_h == 2;
-    for (int i = Gp::rank(); i < n; i += G) c += make_runs(a, sm.hdr, sm.ch, need_a2, r0 + i, &sm.run[2 * i]);
+    for (int i = Gp::rank(); i < n; i += G) {
+        c += make_runs(a, sm.hdr, sm.ch, need_a2, r0 + i, &sm.run[2 * i]);
+        if (aring) {
+            const float st = a.rt.st32[r0 + i];
+            aring[i].sr = sinf((float)(a.rt.theta[r0 + i] - sm.hdr.theta0));
+            aring[i].cr = 2.0f * (float)sm.hdr.z0 * st;
+            aring[i].st2 = 2.0f * st;
+        }
+    }
     c = __reduce_add_sync(0xffffffffu, c);
     if (G > 32) {
         if ((threadIdx.x & 31) == 0) sm.cnt_red[Gp::warp()] = c;
@@ -349,8 +376,9 @@ __device__ inline int build_runs(const DiscArgs &a, CompSmem<RCH> &sm, int r0, i
 }
 
 // Walks the staged rings; lane l handles pixels l and l + 32 of each
-// 64-pixel stretch of a run.  body(run, j, second) gets the first pixel index
-// j and whether j + 32 is inside the run.  In a block, warps claim whole
+// 64-pixel stretch of a run.  body(run, ring, j, second) gets the ring's
+// index in the chunk, the first pixel index j and whether j + 32 is inside
+// the run.  In a block, warps claim whole
 // rings (both run slots: the second only when the ring wrapped) from a shared
 // counter reset by the caller; the next claim is issued before the current
 // ring is walked, so its latency is hidden, and no warp waits at the next
@@ -360,10 +388,10 @@ __device__ inline void run_walk(CompSmem<RCH> &sm, int n, Body body) {
     const int lane = threadIdx.x & 31;
     auto ring = [&](int i) {
         const Run r = sm.run[2 * i];
-        for (int j = lane; j < r.cnt; j += 64) body(r, j, j + 32 < r.cnt);
+        for (int j = lane; j < r.cnt; j += 64) body(r, i, j, j + 32 < r.cnt);
         if (r.more) {
             const Run r2 = sm.run[2 * i + 1];
-            for (int j = lane; j < r2.cnt; j += 64) body(r2, j, j + 32 < r2.cnt);
+            for (int j = lane; j < r2.cnt; j += 64) body(r2, i, j, j + 32 < r2.cnt);
         }
     };
     if (G == 32) {
@@ -414,7 +442,7 @@ __device__ void render_particle(const DiscArgs &a, CompSmem<RCH> &sm, int pidx) 
             if (rk == 0) sm.next_run = 0;
             Gp::sync();
         }
-        run_walk<G, RCH>(sm, n, [&](const Run &r, int j, bool second) {
+        run_walk<G, RCH>(sm, n, [&](const Run &r, int, int j, bool second) {
             const float jf = (float)j;
             float2 w = weight2(e, r, make_float2(jf, jf + 32.0f));
             if (!second) w.y = 0.0f;
@@ -463,7 +491,7 @@ __device__ void render_particle(const DiscArgs &a, CompSmem<RCH> &sm, int pidx) 
             if (rk == 0) sm.next_run = 0;
             Gp::sync();
         }
-        run_walk<G, RCH>(sm, n, [&](const Run &r, int j, bool second) {
+        run_walk<G, RCH>(sm, n, [&](const Run &r, int, int j, bool second) {
             const float jf = (float)j;
             const float2 w = weight2(e, r, make_float2(jf, jf + 32.0f));
             const float2 p = mul2(w, f2(F));
@@ -528,6 +556,175 @@ cudaError_t launch_block(const DiscArgs &a, int num_sms, int blocks_per_sm, cuda
     return cudaGetLastError();
 }
 
+// ------------------------------------------------------------------ adjoint
+// The adjoint of the map (the formulas of adjoint.cu) with the compensated
+// form's FP32 weights.  The tangent vector v_p - cos(alpha) n of each pixel is
+// taken in the particle's local basis (e_theta, e_phi), where
+//   v . e_theta = sin(theta_r - theta0) - 2 cos(theta0) sin(theta_r) sin^2(dphi/2),
+//   v . e_phi   = sin(theta_r) sin(dphi) = 2 sin(theta_r) sin(x) cos(x),  x = dphi/2,
+// both accurate to FP32 relative precision however small alpha is (the 3-D
+// difference v - cos(alpha) n is not); alpha / sin(alpha) =
+// sqrt(g / (h (1 - h))) with h = hav(alpha) and g = alpha^2 / 4 from the
+// weight.  Sums: S with the offset Fast2Sum, the signed ones (sum G w, V_theta,
+// V_phi, T) with Kahan's compensation per lane, all reduced in FP64; the
+// epilogue turns V into the map frame and writes the gradient in FP64.
+template <int RCH>
+struct AdjcSmem {
+    CompSmem<RCH> c;
+    AdjRing aring[RCH];
+    double red[3][32];
+};
+
+__device__ __forceinline__ void kahan(float &s, float &c, float v) {
+    const float y = v - c;
+    const float t = s + y;
+    c = (t - s) - y;
+    s = t;
+}
+
+template <int G, int RCH>
+__device__ void adjc_particle(const adj::AdjArgs &a, AdjcSmem<RCH> &sm, int pidx, double acc[12]) {
+    using Gp = Grp<G>;
+    const DiscArgs &da = a.d;
+    const int rk = Gp::rank();
+    if (rk == 0) {
+        disc_setup(da.g, da.theta[pidx], da.phi[pidx], da.ar[pidx], da.flux[pidx], da.cpix[pidx],
+                   pidx, sm.c.hdr);
+        particle_setup(da.g, sm.c.hdr, sm.c.ext, sm.c.ch);
+    }
+    Gp::sync();
+    const Ext e = sm.c.ext;
+    const int r_first = sm.c.hdr.r_first, r_last = sm.c.hdr.r_last;
+    const int nring = r_last - r_first + 1;
+    const int nchunk = nring > 0 ? (nring + RCH - 1) / RCH : 0;
+    const float *g32 = a.gmap32;
+
+    // pass 1: S (offset Fast2Sum) and sum G w (Kahan)
+    float2 ks = f2(1.0f), kc = f2(0.0f);
+    float as = 0.0f, ac = 0.0f;
+    long long total = 0;
+    for (int c = 0; c < nchunk; c++) {
+        const int r0 = r_first + c * RCH;
+        const int n = min(RCH, r_last - r0 + 1);
+        total += build_runs<G, RCH>(da, sm.c, r0, n, sm.aring);
+        if (G > 32) {
+            if (rk == 0) sm.c.next_run = 0;
+            Gp::sync();
+        }
+        run_walk<G, RCH>(sm.c, n, [&](const Run &r, int, int j, bool second) {
+            const float jf = (float)j;
+            float2 w = weight2(e, r, make_float2(jf, jf + 32.0f));
+            if (!second) w.y = 0.0f;
+            const int pix = r.pix0 + j;
+            const float gw = g32[pix] * w.x + (second ? g32[pix + 32] * w.y : 0.0f);
+            kahan(as, ac, gw);
+            const float2 t = add2(ks, w);
+            kc = add2(kc, sub2(w, sub2(t, ks)));
+            ks = t;
+        });
+        Gp::sync();
+    }
+    double s1[3] = {(((double)ks.x - 1.0) + (double)kc.x) + (((double)ks.y - 1.0) + (double)kc.y),
+                    (double)as - (double)ac, 0.0};
+    adj::group_sum<G, 2>(s1, sm.red);
+    if (total < 2) {  // genmap.cpp:125-128: the whole flux in the centre pixel
+        if (rk == 0) {
+            const double KV[3] = {0.0, 0.0, 0.0};
+            adj::write_grad(a, pidx, a.gmap[sm.c.hdr.cpix] * a.inv_dOmega, 0.0, KV, false, acc);
+            atomicAdd((unsigned long long *)(da.ctr + C_DEPOSITS), 1ull);
+        }
+        Gp::sync();
+        return;
+    }
+    if (rk == 0) atomicAdd((unsigned long long *)(da.ctr + C_DEPOSITS), (unsigned long long)total);
+    const double S = s1[0];
+    const double Gm = s1[1] / S;
+    const float gm = (float)Gm;
+
+    // pass 2: V_theta, V_phi, T with q = (G - Gm) w
+    float vts = 0.0f, vtc = 0.0f, vps = 0.0f, vpc = 0.0f, ts = 0.0f, tc = 0.0f;
+    for (int c = 0; c < nchunk; c++) {
+        const int r0 = r_first + c * RCH;
+        const int n = min(RCH, r_last - r0 + 1);
+        if (nchunk > 1) build_runs<G, RCH>(da, sm.c, r0, n, sm.aring);
+        if (G > 32) {
+            if (rk == 0) sm.c.next_run = 0;
+            Gp::sync();
+        }
+        run_walk<G, RCH>(sm.c, n, [&](const Run &r, int ring, int j, bool second) {
+            const float jf = (float)j;
+            float2 sn, h, g;
+            const float2 w = weight2x(e, r, make_float2(jf, jf + 32.0f), sn, h, g);
+            const AdjRing ar = sm.aring[ring];
+            const int pix = r.pix0 + j;
+            float vt = 0.0f, vp = 0.0f, tt = 0.0f;
+#pragma unroll
+            for (int k = 0; k < 2; k++) {
+                if (k == 1 && !second) break;
+                const float wk = k ? w.y : w.x, snk = k ? sn.y : sn.x, hk = k ? h.y : h.x,
+                            gk = k ? g.y : g.x;
+                const float q = (g32[pix + 32 * k] - gm) * wk;
+                // alpha / sin(alpha); 0 at the antipode, where the tangent is undefined
+                const float om = 1.0f - hk;
+                const float af = hk > 1e-30f ? (om > 1e-7f ? sqrtf(gk / (hk * om)) : 0.0f) : 1.0f;
+                const float s2 = snk * snk;
+                const float eth = fmaf(-ar.cr, s2, ar.sr);
+                const float eph = ar.st2 * snk * sqrtf(fmaxf(1.0f - s2, 0.0f));
+                const float qa = q * af;
+                vt = fmaf(qa, eth, vt);
+                vp = fmaf(qa, eph, vp);
+                tt = fmaf(q, 4.0f * gk, tt);
+            }
+            kahan(vts, vtc, vt);
+            kahan(vps, vpc, vp);
+            kahan(ts, tc, tt);
+        });
+        Gp::sync();
+    }
+    double s2[3] = {(double)vts - (double)vtc, (double)vps - (double)vpc, (double)ts - (double)tc};
+    adj::group_sum<G, 3>(s2, sm.red);
+    if (rk == 0) {
+        const DiscHdr &d = sm.c.hdr;
+        const double ct = cos(d.theta0), st = sin(d.theta0), cp = cos(d.phi0), sp = sin(d.phi0);
+        const double V[3] = {s2[0] * ct * cp - s2[1] * sp, s2[0] * ct * sp + s2[1] * cp, -s2[0] * st};
+        const double K = adj::kInvC2 * d.flux / (S * d.ar * d.ar) * a.inv_dOmega;
+        const double KV[3] = {K * V[0], K * V[1], K * V[2]};
+        adj::write_grad(a, pidx, Gm * a.inv_dOmega, K * s2[2], KV, true, acc);
+    }
+    Gp::sync();
+}
+
+template <int BT, int RCH, int MINB>
+__global__ void __launch_bounds__(BT, MINB) k_adjc_block(adj::AdjArgs a) {
+    __shared__ AdjcSmem<RCH> sm;
+    __shared__ int s_q;
+    double acc[12] = {0.0};
+    const long long nblk = a.d.ctr[C_ADD_BLOCK];
+    for (;;) {
+        if (threadIdx.x == 0) s_q = (int)atomicAdd((unsigned long long *)(a.d.ctr + C_QNEXT_BLOCK), 1ull);
+        __syncthreads();
+        const int q = s_q;
+        __syncthreads();
+        if (q >= nblk) break;
+        adjc_particle<BT, RCH>(a, sm, a.d.queue[q], acc);
+    }
+    if (threadIdx.x == 0) adj::flush_acc(a.oacc, acc);
+}
+
+constexpr int kWPBA = 4;   // warps per block of the adjoint's warp kernel (shared memory)
+
+__global__ void __launch_bounds__(kWPBA * 32) k_adjc_warp(adj::AdjArgs a) {
+    __shared__ AdjcSmem<kRCHW> sm[kWPBA];
+    double acc[12] = {0.0};
+    const long long nblk = a.d.ctr[C_ADD_BLOCK];
+    const long long ndisc = a.d.ctr[C_ADD_DISC];
+    const int w = threadIdx.x >> 5;
+    const long long gw = (long long)blockIdx.x * kWPBA + w;
+    const long long nw = (long long)gridDim.x * kWPBA;
+    for (long long q = nblk + gw; q < ndisc; q += nw) adjc_particle<32, kRCHW>(a, sm[w], a.d.queue[q], acc);
+    if ((threadIdx.x & 31) == 0) adj::flush_acc(a.oacc, acc);
+}
+
 }  // namespace
 
 cudaError_t launch_disc_comp(const DiscArgs &a, int num_sms, int blocks_per_sm, int block_threads,
@@ -543,6 +740,22 @@ cudaError_t launch_disc_comp(const DiscArgs &a, int num_sms, int blocks_per_sm, 
     if (e != cudaSuccess) return e;
     if (occw < 1) occw = 1;
     k_comp_warp<<<num_sms * occw, kWPB * 32, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+// The compensated adjoint's disc kernels (block class, then warp class).
+cudaError_t launch_adjoint_comp_discs(const adj::AdjArgs &a, int num_sms, cudaStream_t s) {
+    int occ = 0;
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_adjc_block<256, 256, 4>, 256, 0);
+    if (e != cudaSuccess) return e;
+    if (occ < 1) occ = 1;
+    k_adjc_block<256, 256, 4><<<num_sms * occ, 256, 0, s>>>(a);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    int occw = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occw, k_adjc_warp, kWPBA * 32, 0);
+    if (e != cudaSuccess) return e;
+    if (occw < 1) occw = 1;
+    k_adjc_warp<<<num_sms * occw, kWPBA * 32, 0, s>>>(a);
     return cudaGetLastError();
 }
 

@@ -104,8 +104,10 @@ cudaError_t launch_disc_comp(const DiscArgs &a, int num_sms, int blocks_per_sm, 
 // [6][n] (x, y, z, m, rho, h); oacc[12] (zeroed by the caller) receives
 // sum_i dL/du_i and dL/drot (row-major).  Needs the prep outputs (with cls)
 // and the disc queue of the same particles and frame.
+// precision: DMANN_PLAIN_F64 (FP64 weights) or DMANN_COMP_F32 (the
+// compensated form's FP32 weights; gmap32 receives gmap rounded, npix floats).
 cudaError_t launch_adjoint(const DiscArgs &d, const Particles &p, const signed char *cls,
-                           const double *gmap, double *grad, double *oacc, int num_sms,
-                           cudaStream_t s);
+                           const double *gmap, float *gmap32, double *grad, double *oacc,
+                           int precision, int num_sms, cudaStream_t s);
 
 }  // namespace dmann

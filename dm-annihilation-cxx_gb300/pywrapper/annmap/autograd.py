@@ -9,8 +9,9 @@
 
 The forward renders the FP64 map of the plain form (or, with
 ``precision=COMP_F32``, the compensated form, which agrees with it to about
-1e-7 per pixel); the backward is the exact adjoint of the plain form with
-every particle's disc pixel set held fixed, recomputing the kernel weights.
+1e-7 per pixel); the backward is the adjoint of the map with every
+particle's disc pixel set held fixed, recomputing the kernel weights in the
+same precision form (FP64, or FP32 weights with compensated sums).
 The observer enters through the rotation set-up of the reference
 (Parameters::setupRotation, src/parameters.cpp:183-289), differentiated with
 respect to the observer position.  Inputs are CUDA tensors (float32
@@ -51,19 +52,20 @@ class SkyMap(torch.autograd.Function):
         r.render(parts, nside, precision, out=out)
         ctx.save_for_backward(x, y, z, m, rho, h)
         ctx.cfg = (dev, op, tuple(cpos), tuple(align), float(unit_factor), float(hires_threshold),
-                   int(nside))
+                   int(nside), int(precision))
         return out
 
     @staticmethod
     def backward(ctx, grad_map):
         x, y, z, m, rho, h = ctx.saved_tensors
-        dev, op, cpos, align, uf, thr, nside = ctx.cfg
+        dev, op, cpos, align, uf, thr, nside, precision = ctx.cfg
         r = _renderer(dev)
         r.set_observer(op, cpos, align)
         r.set_units(uf, thr)
         parts = {"x": x.detach(), "y": y.detach(), "z": z.detach(), "m": m.detach(),
                  "rho": rho.detach(), "h": h.detach()}
-        g, gopos = r.adjoint(parts, nside, grad_map.detach().to(torch.float64).contiguous())
+        g, gopos = r.adjoint(parts, nside, grad_map.detach().to(torch.float64).contiguous(),
+                             precision=precision)
         grads = [g[k].to(t.dtype) if t.requires_grad else None
                  for k, t in enumerate((x, y, z, m, rho, h))]
         gop = torch.as_tensor(np.asarray(gopos), dtype=torch.float64) if ctx.needs_input_grad[6] else None

@@ -208,10 +208,11 @@ class Renderer:
         self._keep = []
         return outs
 
-    def adjoint(self, parts: dict, nside: int, grad_map, out=None):
-        """Gradient of L = sum_p grad_map[p] * map[p] (the plain-form map of
-        ``render`` for this frame and these units) with respect to the particle
-        inputs and the observer position.  Returns (grad, grad_opos): grad is
+    def adjoint(self, parts: dict, nside: int, grad_map, out=None, precision: int = PLAIN_F64):
+        """Gradient of L = sum_p grad_map[p] * map[p] (the map of ``render``
+        for this frame and these units) with respect to the particle inputs and
+        the observer position; precision PLAIN_F64 recomputes the weights in
+        FP64, COMP_F32 with the compensated form's FP32 weights (faster).  Returns (grad, grad_opos): grad is
         [6, n] float64 (rows x, y, z, m, rho, h; a CUDA tensor when the inputs
         are CUDA tensors, else numpy), grad_opos a length-3 numpy array."""
         arrays = [parts[f] for f in FIELDS]
@@ -234,7 +235,8 @@ class Renderer:
         gm = self._ptr(grad_map, np.float64)
         optr = C.c_void_p(out.data_ptr() if _is_torch(out) else out.ctypes.data)
         go = (C.c_double * 3)()
-        self._check(self.L.dmann_adjoint(self.ctx, *ptrs, int(n), int(nside), gm, optr, go))
+        self._check(self.L.dmann_adjoint(self.ctx, *ptrs, int(n), int(nside), int(precision), gm,
+                                         optr, go))
         self._keep = []
         return out, np.array(go[:])
 

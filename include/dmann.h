@@ -240,14 +240,16 @@ dmann_status dmann_render_batch(dmann_ctx *ctx, const float *x, const float *y,
  * and single-pixel decision held fixed (the map is piecewise smooth: it
  * jumps where a pixel centre crosses a disc edge).  Skipped particles (hires
  * mass, rho < 0, invalid geometry) get zero gradient.  The kernel weights are
- * recomputed in FP64, not stored.  The observer gradient includes the
+ * recomputed, not stored: in FP64 with precision DMANN_PLAIN_F64, or with the
+ * compensated form's FP32 weights and compensated sums (per-particle
+ * epilogue in FP64) with DMANN_COMP_F32.  The observer gradient includes the
  * rotation's dependence on the observer when the frame was set by
  * dmann_set_observer; after dmann_set_frame the rotation is held fixed.
  * Blocks until the gradients are written; dmann_get_stats then reports the
  * adjoint's counters and device time. */
 dmann_status dmann_adjoint(dmann_ctx *ctx, const float *x, const float *y,
                            const float *z, const float *m, const float *rho,
-                           const float *h, int64_t n, int nside,
+                           const float *h, int64_t n, int nside, int precision,
                            const double *grad_map, double *grad,
                            double grad_opos[3]);
 
