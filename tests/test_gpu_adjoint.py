@@ -40,6 +40,17 @@ def _normwise(a, b):
     return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
 
 
+def _same(a, b, prec):
+    """Two runs of the same adjoint: bit for bit in FP64 (per-particle sums in
+    a fixed order); the compensated form's per-lane FP32 sums follow the
+    order in which warps claim rings, so they agree to FP32 rounding."""
+    if prec == PLAIN:
+        assert np.array_equal(a, b)
+    else:
+        for k in range(a.shape[0]):
+            assert _normwise(a[k], b[k]) <= 1e-6, k
+
+
 COMP = annmap.COMP_F32
 # agreement with the oracle's FP64 adjoint: norm-wise per field, and observer
 TOL_ORACLE = {PLAIN: 1e-9, COMP: 3e-7}
@@ -108,8 +119,8 @@ def test_adjoint_host_and_device_buffers_agree(case):
     g2, go2 = r.adjoint(tparts, 128, torch.from_numpy(G).cuda(), precision=prec)
     torch.cuda.synchronize()
     r.close()
-    assert np.array_equal(g2.cpu().numpy(), grad)   # per-particle sums have a fixed order
-    assert np.allclose(go2, gopos, rtol=1e-12, atol=0)
+    _same(g2.cpu().numpy(), grad, prec)
+    assert np.allclose(go2, gopos, rtol=1e-12 if prec == PLAIN else 1e-6, atol=0)
 
 
 def test_adjoint_with_fixed_rotation_frame(case):
@@ -121,8 +132,8 @@ def test_adjoint_with_fixed_rotation_frame(case):
     r.set_units(p.unit_factor, p.hires_threshold)
     g2, go2 = r.adjoint(parts, 128, G, precision=prec)
     r.close()
-    assert np.array_equal(g2, grad)
-    assert np.allclose(go2, -grad[:3].sum(axis=1), rtol=1e-10, atol=0)
+    _same(g2, grad, prec)
+    assert np.allclose(go2, -g2[:3].sum(axis=1), rtol=1e-10, atol=0)
 
 
 def test_adjoint_empty_and_invalid_arguments():
@@ -152,8 +163,9 @@ def test_sky_map_autograd_function(case):
     for k, f in enumerate(FIELDS):
         got = t[f].grad.cpu().numpy().astype(np.float64)
         assert t[f].grad.dtype == torch.float32
-        assert _normwise(got, grad[k].astype(np.float32).astype(np.float64)) == 0.0, f
-    assert np.allclose(opos.grad.numpy(), gopos, rtol=1e-12, atol=0)
+        ref = grad[k].astype(np.float32).astype(np.float64)
+        assert _normwise(got, ref) <= (0.0 if prec == PLAIN else 1e-6), f
+    assert np.allclose(opos.grad.numpy(), gopos, rtol=1e-12 if prec == PLAIN else 1e-6, atol=0)
 
 
 @pytest.mark.parametrize("prec", [PLAIN, COMP], ids=["plain", "comp"])
