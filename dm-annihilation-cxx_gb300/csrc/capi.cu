@@ -854,10 +854,22 @@ dmann_status dmann_render_batch(dmann_ctx *ctx, const float *x, const float *y, 
     std::memcpy(opos0, ctx->opos, sizeof opos0);
     const bool had_frame = ctx->have_frame, had_geom = ctx->have_geom;
     // device maps: the whole batch is captured into one CUDA graph and
-    // launched once; host maps go through the context's staging map
+    // launched once; host maps go through the context's staging map.  The
+    // capture runs on the context's own stream (a caller's stream may be the
+    // legacy default stream, which cannot be captured), fenced to the
+    // caller's stream with events on both sides.
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
-    if (all_dev) CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    const cudaStream_t caller = s;
+    if (all_dev) {
+        if (s != ctx->own) {
+            CK(cudaEventRecord(ctx->evdm, s));
+            CK(cudaStreamWaitEvent(ctx->own, ctx->evdm, 0));
+        }
+        s = ctx->own;
+        ctx->stream = s;
+        CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    }
     for (int k = 0; k < n_obs && st == DMANN_OK; k++) {
         std::memcpy(ctx->rot, rot + 9 * k, sizeof(double) * 9);
         std::memcpy(ctx->opos, opos + 3 * k, sizeof(double) * 3);
@@ -876,6 +888,7 @@ dmann_status dmann_render_batch(dmann_ctx *ctx, const float *x, const float *y, 
     ctx->have_geom = had_geom;
     if (all_dev) {
         cudaError_t e = cudaStreamEndCapture(s, &graph);
+        ctx->stream = caller;
         if (st != DMANN_OK) {
             if (graph) cudaGraphDestroy(graph);
             return st;

@@ -72,9 +72,18 @@ class Renderer:
         self._keep.append(arr)
         return C.c_void_p(arr.ctypes.data)
 
+    CUDA_STREAM_LEGACY = 1   # cudaStreamLegacy: the legacy default ("NULL") stream
+
     def set_stream(self, stream=None):
-        """Runs on a cudaStream_t (an int handle or a torch.cuda.Stream)."""
-        h = getattr(stream, "cuda_stream", stream)
+        """Runs on a cudaStream_t: an int handle, or a torch.cuda.Stream (torch's
+        default stream, handle 0, is the legacy default stream); None returns
+        to the context's own stream."""
+        if stream is None:
+            h = None
+        elif hasattr(stream, "cuda_stream"):
+            h = stream.cuda_stream or self.CUDA_STREAM_LEGACY
+        else:
+            h = stream or None
         self._check(self.L.dmann_set_stream(self.ctx, C.c_void_p(h) if h else None))
 
     def _use_torch_stream(self, arrays):

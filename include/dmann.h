@@ -129,7 +129,8 @@ const char *dmann_last_error(const dmann_ctx *ctx);
 int dmann_abi_version(void);
 
 /* Runs subsequent work on `stream` (a cudaStream_t; NULL = the context's
- * own stream).  Lets a caller such as PyTorch share its current stream. */
+ * own stream; the legacy default stream is cudaStreamLegacy).  Lets a caller
+ * such as PyTorch share its current stream. */
 dmann_status dmann_set_stream(dmann_ctx *ctx, void *stream);
 dmann_status dmann_synchronize(dmann_ctx *ctx);
 

@@ -271,3 +271,25 @@ def test_flux_law_needs_velocity_dispersion(rend):
         rend.render(parts, p.map.Nside, COMP)
     rend.set_params(p)   # back to nosom: sigmav not needed
     rend.render(parts, p.map.Nside, COMP)
+
+
+def test_torch_default_stream_orders_the_render():
+    """On torch's default (legacy) stream the render is ordered before torch's
+    next operation without any synchronisation by the caller."""
+    torch = pytest.importorskip("torch")
+    P = synth.nfw_halo(200000, seed=77, n_sub=3)
+    par = annmap.Parameters.for_synthetic(P, 512)
+    r = annmap.Renderer(0)
+    r.set_params(par)
+    d = {k: torch.from_numpy(v).cuda() for k, v in P.as_dict().items()}
+    ref = r.render(P.as_dict(), 512, COMP)          # host map: complete on return
+    out = torch.zeros(12 * 512 * 512, dtype=torch.float64, device="cuda")
+    assert torch.cuda.current_stream().cuda_stream == 0
+    r.render(d, 512, COMP, out=out)                  # queued on torch's stream
+    total = float(out.sum())                         # torch reads it at once
+    assert math.isclose(total, float(ref.sum()), rel_tol=1e-9)
+    maps = [torch.zeros(12 * 64 * 64, dtype=torch.float64, device="cuda") for _ in range(2)]
+    frames = [(np.array(par.rot_flat()), P.obs_pos)] * 2
+    r.render_batch(d, frames, [64, 64], COMP, outs=maps)
+    assert float(maps[1].sum()) > 0 and math.isclose(float(maps[0].sum()), float(maps[1].sum()), rel_tol=1e-9)
+    r.close()
