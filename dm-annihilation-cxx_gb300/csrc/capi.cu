@@ -55,8 +55,7 @@ struct dmann_ctx {
     std::map<int, RingTables> rings;
     // workspace
     DevBuf in[7], theta, phi, ar, flux, cpix, key, queue, hist, ctr, fsum, acc, map;
-    DevBuf cls, oacc, grad;   // particle classes, the adjoint's observer sums, staged gradient
-    DevBuf fixst;             // FixState of the compensated form's fixed-point plane
+    DevBuf cls, oacc, grad;   // the adjoint's class array, observer sums, staged gradient
     // halo cores of the ann_core_nosom law (dmann_set_halo_cores)
     DevBuf halo_f, halo_cells, corr;
     HaloGrid halo{};
@@ -278,7 +277,7 @@ void dmann_destroy(dmann_ctx *ctx) {
                       &ctx->theta, &ctx->phi, &ctx->ar, &ctx->flux, &ctx->cpix, &ctx->key,
                       &ctx->queue, &ctx->hist, &ctx->ctr, &ctx->fsum, &ctx->acc, &ctx->map,
                       &ctx->cls, &ctx->oacc, &ctx->grad, &ctx->halo_f, &ctx->halo_cells,
-                      &ctx->corr, &ctx->fixst};
+                      &ctx->corr};
     for (DevBuf *b : bufs)
         if (b->p) cudaFree(b->p);
     for (auto &kv : ctx->rings) {
@@ -551,9 +550,10 @@ bool law_needs_sigmav(int model) {
 
 Accum make_accum(dmann_ctx *ctx) {
     Accum acc;
+    const size_t P = (size_t)ctx->g.npix;
     acc.acc64 = (double *)ctx->acc.p;
-    acc.fix = (unsigned long long *)ctx->acc.p;
-    acc.fs = (FixState *)ctx->fixst.p;
+    acc.hi = (float *)ctx->acc.p;
+    acc.lo = (float *)ctx->acc.p + P;
     return acc;
 }
 
@@ -574,13 +574,11 @@ dmann_status dmann_map_begin(dmann_ctx *ctx, int nside, int precision) {
     if ((st = ring_tables(ctx, nside, ctx->rt)) != DMANN_OK) return st;
     const size_t P = (size_t)ctx->g.npix;
     if ((st = ensure(ctx, ctx->acc, 8 * P)) || (st = ensure(ctx, ctx->hist, 4 * (size_t)kKeys)) ||
-        (st = ensure(ctx, ctx->ctr, 8 * C_COUNT)) || (st = ensure(ctx, ctx->fsum, 8)) ||
-        (st = ensure(ctx, ctx->fixst, sizeof(FixState))))
+        (st = ensure(ctx, ctx->ctr, 8 * C_COUNT)) || (st = ensure(ctx, ctx->fsum, 8)))
         return st;
     cudaStream_t s = ctx->stream;
     CK(cudaEventRecord(ctx->ev0, s));
     CK(cudaMemsetAsync(ctx->acc.p, 0, 8 * P, s));
-    CK(launch_fix_reset((FixState *)ctx->fixst.p, s));
     CK(cudaMemsetAsync(ctx->ctr.p, 0, 8 * C_COUNT, s));
     CK(cudaMemsetAsync(ctx->fsum.p, 0, 8, s));
     ctx->stats = dmann_stats{};
@@ -611,7 +609,7 @@ dmann_status dmann_map_add_v(dmann_ctx *ctx, const float *x, const float *y, con
     if ((st = ensure(ctx, ctx->theta, 8 * N)) || (st = ensure(ctx, ctx->phi, 8 * N)) ||
         (st = ensure(ctx, ctx->ar, 8 * N)) || (st = ensure(ctx, ctx->flux, 8 * N)) ||
         (st = ensure(ctx, ctx->cpix, 4 * N)) || (st = ensure(ctx, ctx->key, 4 * N)) ||
-        (st = ensure(ctx, ctx->queue, 4 * N)) || (st = ensure(ctx, ctx->cls, N)))
+        (st = ensure(ctx, ctx->queue, 4 * N)))
         return st;
     // inputs: device pointers are used in place, host arrays are copied
     const float *src[7] = {x, y, z, m, rho, h, law_needs_sigmav(ctx->flux_model) ? sigmav : nullptr};
@@ -646,8 +644,7 @@ dmann_status dmann_map_add_v(dmann_ctx *ctx, const float *x, const float *y, con
     pa.f = f;
     pa.g = ctx->g;
     pa.out = {(double *)ctx->theta.p, (double *)ctx->phi.p, (double *)ctx->ar.p,
-              (double *)ctx->flux.p, (int *)ctx->cpix.p, (int *)ctx->key.p,
-              (signed char *)ctx->cls.p};
+              (double *)ctx->flux.p, (int *)ctx->cpix.p, (int *)ctx->key.p};
     pa.hist = (int *)ctx->hist.p;
     pa.ctr = (long long *)ctx->ctr.p;
     pa.flux_sum = (double *)ctx->fsum.p;
@@ -656,7 +653,6 @@ dmann_status dmann_map_add_v(dmann_ctx *ctx, const float *x, const float *y, con
     pa.block_bucket_min = bmin;
     pa.deposit_singles = 1;
     CK(launch_prep(pa, s));
-    if (ctx->precision == DMANN_COMP_F32) CK(launch_fix_chunk(pa, s));
     CK(launch_scan(pa.hist, pa.ctr, bmin, s));
     CK(launch_scatter(pa, (int *)ctx->queue.p, s));
 
@@ -695,7 +691,9 @@ dmann_status dmann_map_end(dmann_ctx *ctx, double *map_out, int accumulate) {
         dmap = (double *)ctx->map.p;
         if (accumulate) CK(cudaMemcpyAsync(dmap, map_out, 8 * P, cudaMemcpyHostToDevice, s));
     }
-    CK(launch_finalize(make_accum(ctx), ctx->precision, ctx->g.npix, ctx->g.dOmega, dmap,
+    double scale;
+    (void)make_frame(ctx, &scale);
+    CK(launch_finalize(make_accum(ctx), ctx->precision, ctx->g.npix, ctx->g.dOmega, scale, dmap,
                        accumulate, s));
     CK(cudaEventRecord(ctx->ev1, s));
     CK(cudaMemcpyAsync(ctx->h_ctr, ctx->ctr.p, 8 * C_COUNT, cudaMemcpyDeviceToHost, s));
@@ -747,7 +745,6 @@ dmann_status issue_observer(dmann_ctx *ctx, const float *const dev[6], int n, in
     CK(cudaMemsetAsync(ctx->acc.p, 0, 8 * P, s));
     CK(cudaMemsetAsync(ctx->ctr.p, 0, 8 * C_COUNT, s));
     CK(cudaMemsetAsync(ctx->fsum.p, 0, 8, s));
-    CK(launch_fix_reset((FixState *)ctx->fixst.p, s));
     double scale;
     const Frame f = make_frame(ctx, &scale);
     const Accum acc = make_accum(ctx);
@@ -761,8 +758,7 @@ dmann_status issue_observer(dmann_ctx *ctx, const float *const dev[6], int n, in
         pa.f = f;
         pa.g = ctx->g;
         pa.out = {(double *)ctx->theta.p, (double *)ctx->phi.p, (double *)ctx->ar.p,
-                  (double *)ctx->flux.p, (int *)ctx->cpix.p, (int *)ctx->key.p,
-                  (signed char *)ctx->cls.p};
+                  (double *)ctx->flux.p, (int *)ctx->cpix.p, (int *)ctx->key.p};
         pa.hist = (int *)ctx->hist.p;
         pa.ctr = (long long *)ctx->ctr.p;
         pa.flux_sum = (double *)ctx->fsum.p;
@@ -771,7 +767,6 @@ dmann_status issue_observer(dmann_ctx *ctx, const float *const dev[6], int n, in
         pa.block_bucket_min = bmin;
         pa.deposit_singles = 1;
         CK(launch_prep(pa, s));
-        if (precision == DMANN_COMP_F32) CK(launch_fix_chunk(pa, s));
         CK(launch_scan(pa.hist, pa.ctr, bmin, s));
         CK(launch_scatter(pa, (int *)ctx->queue.p, s));
         DiscArgs da;
@@ -789,8 +784,7 @@ dmann_status issue_observer(dmann_ctx *ctx, const float *const dev[6], int n, in
         if (precision == DMANN_PLAIN_F64) CK(launch_disc_plain(da, ctx->num_sms, tu.blocks_per_sm, s, nullptr));
         else CK(launch_disc_comp(da, ctx->num_sms, tu.blocks_per_sm, tu.block_threads, s, nullptr));
     }
-    (void)scale;
-    CK(launch_finalize(acc, precision, ctx->g.npix, ctx->g.dOmega, dmap, 0, s));
+    CK(launch_finalize(acc, precision, ctx->g.npix, ctx->g.dOmega, scale, dmap, 0, s));
     return DMANN_OK;
 }
 
@@ -830,8 +824,7 @@ dmann_status dmann_render_batch(dmann_ctx *ctx, const float *x, const float *y, 
         (st = ensure(ctx, ctx->cpix, 4 * n1)) || (st = ensure(ctx, ctx->key, 4 * n1)) ||
         (st = ensure(ctx, ctx->queue, 4 * n1)) || (st = ensure(ctx, ctx->hist, 4 * (size_t)kKeys)) ||
         (st = ensure(ctx, ctx->ctr, 8 * C_COUNT)) || (st = ensure(ctx, ctx->fsum, 8)) ||
-        (st = ensure(ctx, ctx->acc, 8 * Pmax)) || (st = ensure(ctx, ctx->map, 8 * Pmax)) ||
-        (st = ensure(ctx, ctx->cls, n1)) || (st = ensure(ctx, ctx->fixst, sizeof(FixState))))
+        (st = ensure(ctx, ctx->acc, 8 * Pmax)) || (st = ensure(ctx, ctx->map, 8 * Pmax)))
         return st;
     std::vector<RingTables> rts(n_obs);
     for (int k = 0; k < n_obs; k++)

@@ -27,7 +27,7 @@ struct Frame {
     double opos[3];
     double unit_factor;
     double hires_threshold;
-    double inv_scale;     // unused (the fixed-point exponent lives on the device)
+    double inv_scale;     // power of two applied to fluxes deposited in FP32
     int flux_model;       // dmann_flux
     double vel_to_cgs;    // code velocity unit (somv, somv2, pwave laws)
     double fcpos[3];      // halo centre (adiabatic law)
@@ -287,14 +287,6 @@ __device__ inline void deposit2f(float *hi, float *lo, int pix, float v, float e
     float err = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(v, bb));
     err = __fadd_rn(err, extra);
     if (err != 0.0f) red_add_f32(lo + pix, err);
-}
-
-// One fixed-point deposit of v (a non-negative value in plane units, <
-// 2^62) held as the unevaluated FP32 sum p + pe: each part rounded to an
-// integer, added with one non-returning 64-bit reduction.
-__device__ inline void deposit_fix(unsigned long long *plane, int pix, float p, float pe) {
-    const long long i = __float2ll_rn(p) + __float2ll_rn(pe);
-    atomicAdd(plane + pix, (unsigned long long)i);
 }
 
 // ---------------------------------------------------------------- reductions

@@ -16,17 +16,16 @@
 //
 // Normalisation: a compensated FP32 sum per thread (offset so that Fast2Sum
 // captures every rounding error exactly), reduced in FP64.
-// Deposits: a 64-bit fixed-point plane in units of flux * 2^E (E per map,
-// from the kept flux); each deposit w * F/S is formed as p + pe in FP32 (pe the
-// product's exact rounding error and the low part of F/S), the two parts
-// rounded to integers and added with one non-returning 64-bit reduction.
+// Deposits: two FP32 planes (hi, lo); the hi atomic returns the old value, so
+// the exact TwoSum error of each addition -- plus the product's own rounding
+// error and the low part of flux/norm -- goes to the lo plane.
 //
 // Work layout ("run engine"): the disc's rings are staged in shared memory
 // as runs -- one ring's in-disc pixels, split where the ring wraps so that a
 // run is contiguous in the map -- and each warp takes whole runs.  A lane
 // evaluates two pixels of a run at once (j and j + 32) with the packed FP32x2
 // instructions of sm_100+ (__ffma2_rn & co.), halving the issue slots of the
-// polynomial and compensated-sum arithmetic.
+// polynomial, Kahan and TwoSum arithmetic.
 //
 // Polynomials (written from their Taylor series), the number of terms chosen
 // per particle from the largest |x| and h its disc can reach:
@@ -463,27 +462,27 @@ __device__ void render_particle(const DiscArgs &a, CompSmem<RCH> &sm, int pidx) 
         for (int k = 0; k < Gp::kWarps; k++) S += sm.red[k];
         Gp::sync();
     }
-    const int E = a.acc.fs->E;   // fixed-point exponent of the plane
     if (total < 2) {  // genmap.cpp:125-128: the whole flux into the centre pixel
         if (rk == 0) {
-            atomicAdd(a.acc.fix + sm.hdr.cpix, (unsigned long long)__double2ll_rn(ldexp(sm.hdr.flux, E)));
+            const double vs = sm.hdr.flux * a.f.inv_scale;
+            const float vh = (float)vs;
+            const float vl = (float)(vs - (double)vh);
+            deposit2f(a.acc.hi, a.acc.lo, sm.hdr.cpix, vh);
+            if (vl != 0.0f) red_add_f32(a.acc.lo + sm.hdr.cpix, vl);
             atomicAdd((unsigned long long *)(a.ctr + C_DEPOSITS), 1ull);
         }
         Gp::sync();
         return;
     }
     if (rk == 0) atomicAdd((unsigned long long *)(a.ctr + C_DEPOSITS), (unsigned long long)total);
-    // flux / norm in plane units as a two-float
-    const double Fd = ldexp(sm.hdr.flux, E) / S;
+    // flux / norm as a two-float
+    const double Fd = sm.hdr.flux * a.f.inv_scale / S;
     const float F = (float)Fd, Flo = (float)(Fd - (double)F);
-    unsigned long long *const plane = a.acc.fix;
+    float *const hi = a.acc.hi, *const lo = a.acc.lo;
 
-    // pass 2: deposits.  w*F as p + pe, pe the product's rounding error
-    // (exact, from an FMA) plus w*Flo; both parts rounded to plane units and
-    // added with one non-returning 64-bit integer reduction.  Integer sums
-    // do not depend on the order of the additions: the map is reproducible
-    // bit for bit, and a particle's deposits add up to its flux to the plane
-    // unit (2^-62 of the map's total) per pixel.
+    // pass 2: deposits.  w*F as hi + lo: the product's rounding error (exact,
+    // from an FMA) and w*Flo go to the lo plane with the TwoSum error of the
+    // hi atomic, so a particle's deposits add up to its flux to ~1e-12.
     for (int c = 0; c < nchunk; c++) {
         const int r0 = r_first + c * RCH;
         const int n = min(RCH, r_last - r0 + 1);
@@ -498,8 +497,16 @@ __device__ void render_particle(const DiscArgs &a, CompSmem<RCH> &sm, int pidx) 
             const float2 p = mul2(w, f2(F));
             const float2 pe = fma2(w, f2(Flo), fma2(w, f2(F), make_float2(-p.x, -p.y)));
             const int pix = r.pix0 + j;
-            deposit_fix(plane, pix, p.x, pe.x);
-            if (second) deposit_fix(plane, pix + 32, p.y, pe.y);
+            const float a0 = atom_add_f32(hi + pix, p.x);
+            const float a1 = second ? atom_add_f32(hi + pix + 32, p.y) : 0.0f;
+            const float2 av = make_float2(a0, a1);
+            const float2 pv = make_float2(p.x, second ? p.y : 0.0f);
+            const float2 s = add2(av, pv);
+            const float2 bb = sub2(s, av);
+            float2 err = add2(sub2(av, sub2(s, bb)), sub2(pv, bb));
+            err = add2(err, pe);
+            red_add_f32(lo + pix, err.x);
+            if (second) red_add_f32(lo + pix + 32, err.y);
         });
         Gp::sync();
     }

@@ -43,20 +43,9 @@ struct PrepOut {
 // Particle classes written to PrepOut::cls.
 enum PClass : signed char { PC_SKIPPED = 0, PC_INVALID = 1, PC_SINGLE = 2, PC_DISC = 3 };
 
-// Fixed-point state of the compensated form's map: the plane holds
-// integers in units of flux * 2^E (E chosen from the running kept flux so the
-// sum stays below 2^62; lowered, with the plane shifted right, when a later
-// chunk needs it).
-struct FixState {
-    int E;              // current exponent; kFixUnset before the first chunk
-    int shift;          // right shift the plane needs before this chunk's deposits
-};
-constexpr int kFixUnset = -0x7fffffff;
-
 struct Accum {
-    double *acc64;              // DMANN_PLAIN_F64: FP64 plane
-    unsigned long long *fix;    // DMANN_COMP_F32: 64-bit fixed-point plane
-    FixState *fs;               // its exponent
+    double *acc64;      // DMANN_PLAIN_F64
+    float *hi, *lo;     // DMANN_COMP_F32 (compensated two-float planes)
 };
 
 // Halo cores of the ann_core_nosom law, bucketed into a uniform grid whose
@@ -99,13 +88,7 @@ cudaError_t launch_prep(const PrepArgs &a, cudaStream_t s);
 cudaError_t launch_scan(int *hist, long long *ctr, int block_bucket_min, cudaStream_t s);
 cudaError_t launch_scatter(const PrepArgs &a, int *queue, cudaStream_t s);
 cudaError_t launch_finalize(const Accum &acc, int precision, int npix, double dOmega,
-                            double *out, int accumulate, cudaStream_t s);
-// Compensated form, after k_prep of a chunk: choose the fixed-point exponent
-// from the running kept flux (flux_sum), shift the plane if it dropped, and
-// deposit the chunk's single-pixel particles (cls == PC_SINGLE).
-cudaError_t launch_fix_chunk(const PrepArgs &a, cudaStream_t s);
-// Marks the fixed-point exponent unset (a new map).
-cudaError_t launch_fix_reset(FixState *fs, cudaStream_t s);
+                            double scale, double *out, int accumulate, cudaStream_t s);
 // halocore.cu: corr[i] = the halo-core factor r of particle i
 cudaError_t launch_halo_core(const HaloGrid &g, const Particles &p, double *corr, cudaStream_t s);
 // disc_plain.cu / disc_comp.cu

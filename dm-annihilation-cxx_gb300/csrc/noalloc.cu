@@ -66,7 +66,7 @@ __global__ void k_ring_tables(int nside, double fact1, double fact2, double *z, 
 
 // Byte offsets of the scratch regions for n particles at one Nside.
 struct Layout {
-    size_t ring, hist, ctr, fsum, acc, theta, phi, ar, flux, cpix, key, queue, cls, total;
+    size_t ring, hist, ctr, fsum, acc, theta, phi, ar, flux, cpix, key, queue, total;
 };
 
 size_t up256(size_t v) { return (v + 255) & ~(size_t)255; }
@@ -78,8 +78,8 @@ Layout layout(size_t n, int nside) {
     L.ring = o;  o = up256(o + (4 * sizeof(double) + 2 * sizeof(float)) * 4 * (size_t)nside);
     L.hist = o;  o = up256(o + sizeof(int) * (size_t)kKeys);
     L.ctr = o;   o = up256(o + sizeof(long long) * C_COUNT);
-    L.fsum = o;  o = up256(o + sizeof(double) + sizeof(FixState));   // flux sum, then FixState
-    L.acc = o;   o = up256(o + sizeof(unsigned long long) * npix);
+    L.fsum = o;  o = up256(o + sizeof(double));
+    L.acc = o;   o = up256(o + 2 * sizeof(float) * npix);
     L.theta = o; o = up256(o + 8 * n);
     L.phi = o;   o = up256(o + 8 * n);
     L.ar = o;    o = up256(o + 8 * n);
@@ -87,7 +87,6 @@ Layout layout(size_t n, int nside) {
     L.cpix = o;  o = up256(o + 4 * n);
     L.key = o;   o = up256(o + 4 * n);
     L.queue = o; o = up256(o + 4 * n);
-    L.cls = o;   o = up256(o + n);
     L.total = o;
     return L;
 }
@@ -190,22 +189,22 @@ extern "C" dmann_status dmann_render_noalloc(const float *x, const float *y, con
     }
     f.unit_factor = unit_factor;
     f.hires_threshold = hires_threshold;
-    f.inv_scale = 1.0;
+    int e2 = 0;
+    std::frexp(unit_factor, &e2);
+    f.inv_scale = std::ldexp(1.0, -e2);
+    const double scale = std::ldexp(1.0, e2);
     f.flux_model = DMANN_FLUX_ANN_NOSOM;
-    f.vel_to_cgs = 0.0;
-    f.fcpos[0] = f.fcpos[1] = f.fcpos[2] = 0.0;
 
     Accum acc;
     acc.acc64 = nullptr;
-    acc.fix = (unsigned long long *)(b + L.acc);
-    acc.fs = (FixState *)(b + L.fsum + sizeof(double));
+    acc.hi = (float *)(b + L.acc);
+    acc.lo = acc.hi + npix;
 
     // the array keeps the previous call's contents: clear what must start at zero
     NA_CK(cudaMemsetAsync(b + L.hist, 0, sizeof(int) * (size_t)kKeys, s));
     NA_CK(cudaMemsetAsync(b + L.ctr, 0, sizeof(long long) * C_COUNT, s));
     NA_CK(cudaMemsetAsync(b + L.fsum, 0, sizeof(double), s));
-    NA_CK(cudaMemsetAsync(b + L.acc, 0, sizeof(unsigned long long) * (size_t)npix, s));
-    NA_CK(launch_fix_reset(acc.fs, s));
+    NA_CK(cudaMemsetAsync(b + L.acc, 0, 2 * sizeof(float) * (size_t)npix, s));
     k_ring_tables<<<(4 * nside + 255) / 256, 256, 0, s>>>(nside, g.fact1, g.fact2, rz, rst, rth,
                                                           rstep, rst32, rstep32);
     NA_CK(cudaGetLastError());
@@ -216,8 +215,7 @@ extern "C" dmann_status dmann_render_noalloc(const float *x, const float *y, con
         pa.f = f;
         pa.g = g;
         pa.out = {(double *)(b + L.theta), (double *)(b + L.phi), (double *)(b + L.ar),
-                  (double *)(b + L.flux), (int *)(b + L.cpix), (int *)(b + L.key),
-                  (signed char *)(b + L.cls)};
+                  (double *)(b + L.flux), (int *)(b + L.cpix), (int *)(b + L.key)};
         pa.hist = (int *)(b + L.hist);
         pa.ctr = (long long *)(b + L.ctr);
         pa.flux_sum = (double *)(b + L.fsum);
@@ -227,7 +225,6 @@ extern "C" dmann_status dmann_render_noalloc(const float *x, const float *y, con
         pa.deposit_singles = 1;
         pa.core_corr = nullptr;
         NA_CK(launch_prep(pa, s));
-        NA_CK(launch_fix_chunk(pa, s));
         NA_CK(launch_scan(pa.hist, pa.ctr, pa.block_bucket_min, s));
         NA_CK(launch_scatter(pa, (int *)(b + L.queue), s));
         DiscArgs da;
@@ -244,6 +241,6 @@ extern "C" dmann_status dmann_render_noalloc(const float *x, const float *y, con
         da.acc = acc;
         NA_CK(launch_disc_comp(da, sms, 0, 256, s, nullptr));
     }
-    NA_CK(launch_finalize(acc, DMANN_COMP_F32, npix, g.dOmega, map_out, accumulate, s));
+    NA_CK(launch_finalize(acc, DMANN_COMP_F32, npix, g.dOmega, scale, map_out, accumulate, s));
     return DMANN_OK;
 }

@@ -1,6 +1,5 @@
 // prep.cu -- per-particle preparation, single-pixel deposits, the disc work
-// queue (counting sort by size bucket and sky cell), the compensated form's
-// fixed-point scale, and the final map pass.
+// queue (counting sort by size bucket and sky cell) and the final map pass.
 //
 // Compiled with -fmad=false: the per-particle FP64 geometry below repeats
 // the reference CPU path's operations in the same order, unfused, so d, the
@@ -173,12 +172,22 @@ __global__ void __launch_bounds__(256) k_prep(PrepArgs a) {
     // total kept flux (the reference's "Total Conts", genmap.cpp:161-172)
     double fs = warp_sum(kept ? flux : 0.0);
     if ((threadIdx.x & 31) == 0 && fs != 0.0) atomicAdd(a.flux_sum, fs);
-    // single-pixel particles: all their flux into the centre pixel (the
-    // compensated form's go to its fixed-point plane in k_fix_singles, once
-    // the exponent is known)
-    if (a.deposit_singles && a.precision == 0) {
+    // single-pixel particles: all their flux into the centre pixel
+    if (!a.deposit_singles) {
+        // classification only
+    } else if (a.precision == 0) {
         double *acc = a.acc.acc64;
         aggregated_add(single, cpix, flux, [acc](int p, double v) { red_add_f64(acc + p, v); });
+    } else {
+        float *hi = a.acc.hi, *lo = a.acc.lo;
+        const double sc = a.f.inv_scale;
+        aggregated_add(single, cpix, flux, [hi, lo, sc](int p, double v) {
+            double vs = v * sc;
+            float vh = (float)vs;
+            float vl = (float)(vs - (double)vh);
+            deposit2f(hi, lo, p, vh);
+            if (vl != 0.0f) red_add_f32(lo + p, vl);
+        });
     }
     count_warp(a.ctr + C_DEPOSITS, single);
 }
@@ -243,51 +252,17 @@ __global__ void __launch_bounds__(256) k_scatter(const int *key, int n, int *off
 }
 
 // map_out = (accumulate ? map_out : 0) + acc / dOmega   (genmap.cpp:168)
-__global__ void k_finalize(Accum acc, int precision, int npix, double dOmega, double *out,
-                           int accumulate) {
-    const double scale = precision == 0 || acc.fs->E == kFixUnset ? 1.0 : ldexp(1.0, -acc.fs->E);
+__global__ void k_finalize(Accum acc, int precision, int npix, double dOmega, double scale,
+                           double *out, int accumulate) {
     for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < npix; p += gridDim.x * blockDim.x) {
         double v;
         if (precision == 0) {
             v = acc.acc64[p] / dOmega;
         } else {
-            v = (double)(long long)acc.fix[p] * scale / dOmega;
+            v = ((double)acc.hi[p] + (double)acc.lo[p]) * scale / dOmega;
         }
         out[p] = accumulate ? out[p] + v : v;
     }
-}
-
-// The fixed-point exponent for the running kept flux T: T * 2^E < 2^62.
-__global__ void k_fix_scale(const double *flux_sum, FixState *fs) {
-    const double T = *flux_sum;
-    int e = 0;
-    if (T > 0.0) frexp(T, &e);          // T < 2^e
-    fs->shift = 0;
-    if (!(T > 0.0)) {
-        if (fs->E == kFixUnset) fs->E = 0;
-        return;
-    }
-    const int En = 62 - e;
-    if (fs->E == kFixUnset) {
-        fs->E = En;
-    } else if (En < fs->E) {
-        fs->shift = fs->E - En;
-        fs->E = En;
-    }
-}
-
-__global__ void k_fix_shift(unsigned long long *plane, int npix, const FixState *fs) {
-    const int sh = fs->shift;
-    if (sh == 0) return;
-    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < npix; p += gridDim.x * blockDim.x)
-        plane[p] = sh >= 63 ? 0ull : (unsigned long long)((long long)plane[p] >> sh);
-}
-
-__global__ void __launch_bounds__(256) k_fix_singles(PrepArgs a) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= a.p.n || a.out.cls[i] != PC_SINGLE) return;
-    const double v = ldexp(a.out.flux[i], a.acc.fs->E);
-    atomicAdd(a.acc.fix + a.out.cpix[i], (unsigned long long)__double2ll_rn(v));
 }
 
 }  // namespace
@@ -309,33 +284,11 @@ cudaError_t launch_scatter(const PrepArgs &a, int *queue, cudaStream_t s) {
     return cudaGetLastError();
 }
 
-cudaError_t launch_finalize(const Accum &acc, int precision, int npix, double dOmega,
+cudaError_t launch_finalize(const Accum &acc, int precision, int npix, double dOmega, double scale,
                             double *out, int accumulate, cudaStream_t s) {
     int blocks = (npix + 255) / 256;
     if (blocks > 152 * 16) blocks = 152 * 16;
-    k_finalize<<<blocks, 256, 0, s>>>(acc, precision, npix, dOmega, out, accumulate);
-    return cudaGetLastError();
-}
-
-__global__ void k_fix_reset(FixState *fs) {
-    fs->E = kFixUnset;
-    fs->shift = 0;
-}
-
-cudaError_t launch_fix_reset(FixState *fs, cudaStream_t s) {
-    k_fix_reset<<<1, 1, 0, s>>>(fs);
-    return cudaGetLastError();
-}
-
-cudaError_t launch_fix_chunk(const PrepArgs &a, cudaStream_t s) {
-    k_fix_scale<<<1, 1, 0, s>>>(a.flux_sum, a.acc.fs);
-    cudaError_t e = cudaGetLastError();
-    if (e != cudaSuccess) return e;
-    int blocks = (a.g.npix + 255) / 256;
-    if (blocks > 152 * 16) blocks = 152 * 16;
-    k_fix_shift<<<blocks, 256, 0, s>>>(a.acc.fix, a.g.npix, a.acc.fs);
-    if ((e = cudaGetLastError()) != cudaSuccess) return e;
-    if (a.p.n > 0) k_fix_singles<<<(a.p.n + 255) / 256, 256, 0, s>>>(a);
+    k_finalize<<<blocks, 256, 0, s>>>(acc, precision, npix, dOmega, scale, out, accumulate);
     return cudaGetLastError();
 }
 

@@ -272,7 +272,7 @@ dmann_status dmann_get_stats(const dmann_ctx *ctx, dmann_stats *out);
  * dmann_set_frame and dmann_set_units take.  Work is queued on `stream`
  * (a cudaStream_t, NULL = the default stream) of the current device and the
  * call returns without waiting.  The scratch needed is about
- *     8 * 12*nside^2 + 45 * n + 160 * nside + 513 KiB   bytes;
+ *     8 * 12*nside^2 + 44 * n + 160 * nside + 513 KiB   bytes;
  * a larger problem is rejected with DMANN_ERR_TOO_LARGE (render it in chunks
  * of particles with accumulate = 1).  The first call on a device looks up the
  * array's device address (cudaGetSymbolAddress); make that first call before
@@ -292,9 +292,8 @@ dmann_status dmann_render_noalloc(const float *x, const float *y, const float *z
 typedef enum {
     DMANN_PEAK_RED_F32 = 0,   /* red.global.add.f32 */
     DMANN_PEAK_RED_F64 = 1,   /* red.global.add.f64 */
-    DMANN_PEAK_COMP_F32 = 2,  /* the compensated deposit: returning FP32 atomic
+    DMANN_PEAK_COMP_F32 = 2   /* the compensated deposit: returning FP32 atomic
                                  add, exact TwoSum error, FP32 red of the error */
-    DMANN_PEAK_RED_U64 = 3    /* red.global.add.u64 */
 } dmann_peak_kind;
 /* No reference counterpart.  Measures the rate (operations per second) of
  * one kind of global reduction on `device`: a grid of 8 blocks per SM sweeps
