@@ -8,6 +8,7 @@
 // `reps` times.  Kinds:
 //   DMANN_PEAK_RED_F32   red.global.add.f32 (no return value)
 //   DMANN_PEAK_RED_F64   red.global.add.f64
+//   DMANN_PEAK_RED_U64   red.global.add.u64 (an atomicAdd whose value is unused)
 //   DMANN_PEAK_COMP_F32  the compensated deposit: atom.global.add.f32 that
 //                        returns the old value, the exact TwoSum error and a
 //                        red.global.add.f32 of the error into a second plane
@@ -29,6 +30,8 @@ __global__ void __launch_bounds__(256) k_sweep(void *buf, long long n, int reps,
                 red_add_f32((float *)buf + i, v);
             } else if (KIND == DMANN_PEAK_RED_F64) {
                 red_add_f64((double *)buf + i, (double)v);
+            } else if (KIND == DMANN_PEAK_RED_U64) {
+                atomicAdd((unsigned long long *)buf + i, (unsigned long long)(v * 1048576.0f));
             } else {
                 deposit2f((float *)buf, (float *)buf + n, (int)i, v);
             }
@@ -45,7 +48,8 @@ extern "C" dmann_status dmann_measure_l2_red(int device, int kind, int64_t bytes
                                              double *ops_per_s) {
     if (!ops_per_s || reps < 1 || bytes < (1 << 20) || bytes > ((int64_t)1 << 34))
         return DMANN_ERR_INVALID;
-    if (kind != DMANN_PEAK_RED_F32 && kind != DMANN_PEAK_RED_F64 && kind != DMANN_PEAK_COMP_F32)
+    if (kind != DMANN_PEAK_RED_F32 && kind != DMANN_PEAK_RED_F64 && kind != DMANN_PEAK_COMP_F32 &&
+        kind != DMANN_PEAK_RED_U64)
         return DMANN_ERR_INVALID;
     if (cudaSetDevice(device) != cudaSuccess) {
         cudaGetLastError();
@@ -59,7 +63,7 @@ extern "C" dmann_status dmann_measure_l2_red(int device, int kind, int64_t bytes
         cudaGetLastError();
         return DMANN_ERR_NOMEM;
     }
-    const long long elem = kind == DMANN_PEAK_RED_F64 ? 8 : 4;
+    const long long elem = (kind == DMANN_PEAK_RED_F64 || kind == DMANN_PEAK_RED_U64) ? 8 : 4;
     const long long n = kind == DMANN_PEAK_COMP_F32 ? bytes / (2 * elem) : bytes / elem;
     if (kind == DMANN_PEAK_COMP_F32 && n > 0x7fffffffLL) {
         cudaFree(buf);
@@ -80,6 +84,7 @@ extern "C" dmann_status dmann_measure_l2_red(int device, int kind, int64_t bytes
         auto launch = [&](int r) {
             if (kind == DMANN_PEAK_RED_F32) k_sweep<DMANN_PEAK_RED_F32><<<grid, 256, 0, s>>>(buf, n, r, v);
             else if (kind == DMANN_PEAK_RED_F64) k_sweep<DMANN_PEAK_RED_F64><<<grid, 256, 0, s>>>(buf, n, r, v);
+            else if (kind == DMANN_PEAK_RED_U64) k_sweep<DMANN_PEAK_RED_U64><<<grid, 256, 0, s>>>(buf, n, r, v);
             else k_sweep<DMANN_PEAK_COMP_F32><<<grid, 256, 0, s>>>(buf, n, r, v);
         };
         launch(1);  // warm-up
