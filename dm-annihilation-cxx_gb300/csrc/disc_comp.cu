@@ -36,6 +36,8 @@
 //   4h^4/35 + 128h^5/1575 + ... ; three terms for h < 4e-3 (error < 7.4e-9
 //   relative), five for h < 0.02 (< 3e-10); otherwise asinf(sqrtf(h)) from
 //   the CUDA math library.  All truncation errors stay below FP32 rounding.
+#include <type_traits>
+
 #include "adjoint_common.cuh"
 #include "kernels.cuh"
 
@@ -282,14 +284,20 @@ __device__ inline float g_general(float h, float x, const Run &r) {
 
 // Weights of pixels jj = (j, j + 32) of run r; also sin(x) (x half the
 // azimuth offset), the haversine h of the distance and g = theta^2 / 4.
+// TX, TH >= 0 fix the polynomial tiers at compile time (the disc kernels
+// dispatch on the particle's tiers once, outside the pixel loops); -1 reads
+// them from e.
+template <int TX = -1, int TH = -1>
 __device__ __forceinline__ float2 weight2x(const Ext &e, const Run &r, float2 jj, float2 &sn_out,
                                           float2 &h_out, float2 &g_out) {
+    const int tier_x = TX >= 0 ? TX : e.tier_x;
+    const int tier_h = TH >= 0 ? TH : e.tier_h;
     const float2 x = fma2(jj, f2(r.steph), f2(r.d0h));
     const float2 x2 = mul2(x, x);
     float2 p;
-    if (e.tier_x == 0) {
+    if (tier_x == 0) {
         p = fma2(x2, f2(-1.0f / 6.0f), f2(1.0f));
-    } else if (e.tier_x == 1) {
+    } else if (tier_x == 1) {
         p = fma2(x2, f2(-1.0f / 5040.0f), f2(1.0f / 120.0f));
         p = fma2(x2, p, f2(-1.0f / 6.0f));
         p = fma2(x2, p, f2(1.0f));
@@ -305,11 +313,11 @@ __device__ __forceinline__ float2 weight2x(const Ext &e, const Run &r, float2 jj
     const float2 sn = mul2(x, p);
     const float2 h = fma2(f2(r.B), mul2(sn, sn), f2(r.A));
     float2 g;
-    if (e.tier_h == 0) {
+    if (tier_h == 0) {
         float2 q = fma2(h, f2(8.0f / 45.0f), f2(1.0f / 3.0f));
         q = fma2(h, q, f2(1.0f));
         g = mul2(h, q);
-    } else if (e.tier_h == 1) {
+    } else if (tier_h == 1) {
         float2 q = fma2(h, f2(128.0f / 1575.0f), f2(4.0f / 35.0f));
         q = fma2(h, q, f2(8.0f / 45.0f));
         q = fma2(h, q, f2(1.0f / 3.0f));
@@ -325,9 +333,29 @@ __device__ __forceinline__ float2 weight2x(const Ext &e, const Run &r, float2 jj
     return make_float2(ex2_approx(t.x), ex2_approx(t.y));
 }
 
+template <int TX = -1, int TH = -1>
 __device__ __forceinline__ float2 weight2(const Ext &e, const Run &r, float2 jj) {
     float2 sn, h, g;
-    return weight2x(e, r, jj, sn, h, g);
+    return weight2x<TX, TH>(e, r, jj, sn, h, g);
+}
+
+// Calls f(integral_constant<TX>, integral_constant<TH>) with the particle's
+// tiers as constants where both are below 2 (the common small discs), else
+// with -1 (tiers read at run time): five instantiations of f instead of nine.
+template <class F>
+__device__ __forceinline__ void with_tiers(const Ext &e, F f) {
+    using I0 = std::integral_constant<int, 0>;
+    using I1 = std::integral_constant<int, 1>;
+    using IR = std::integral_constant<int, -1>;
+    if (e.tier_x < 2 && e.tier_h < 2) {
+        if (e.tier_x == 0) {
+            if (e.tier_h == 0) f(I0{}, I0{}); else f(I0{}, I1{});
+        } else {
+            if (e.tier_h == 0) f(I1{}, I0{}); else f(I1{}, I1{});
+        }
+    } else {
+        f(IR{}, IR{});
+    }
 }
 
 template <int G>
@@ -409,18 +437,12 @@ __device__ inline void run_walk(CompSmem<RCH> &sm, int n, Body body) {
     }
 }
 
-// Renders one particle with a group of G threads (a warp or a block).
-template <int G, int RCH>
-__device__ void render_particle(const DiscArgs &a, CompSmem<RCH> &sm, int pidx) {
+// Both passes of one disc particle (tiers TX, TH; see weight2x), after
+// render_particle has staged its header.
+template <int G, int RCH, int TX, int TH>
+__device__ void render_disc(const DiscArgs &a, CompSmem<RCH> &sm, const Ext &e) {
     using Gp = Grp<G>;
     const int rk = Gp::rank();
-    if (rk == 0) {
-        disc_setup(a.g, a.theta[pidx], a.phi[pidx], a.ar[pidx], a.flux[pidx], a.cpix[pidx], pidx,
-                   sm.hdr);
-        particle_setup(a.g, sm.hdr, sm.ext, sm.ch);
-    }
-    Gp::sync();
-    const Ext e = sm.ext;
     const int r_first = sm.hdr.r_first, r_last = sm.hdr.r_last;
     const int nring = r_last - r_first + 1;
     const int nchunk = nring > 0 ? (nring + RCH - 1) / RCH : 0;
@@ -444,7 +466,7 @@ __device__ void render_particle(const DiscArgs &a, CompSmem<RCH> &sm, int pidx) 
         }
         run_walk<G, RCH>(sm, n, [&](const Run &r, int, int j, bool second) {
             const float jf = (float)j;
-            float2 w = weight2(e, r, make_float2(jf, jf + 32.0f));
+            float2 w = weight2<TX, TH>(e, r, make_float2(jf, jf + 32.0f));
             if (!second) w.y = 0.0f;
             const float2 t = add2(ks, w);
             kc = add2(kc, sub2(w, sub2(t, ks)));
@@ -493,7 +515,7 @@ __device__ void render_particle(const DiscArgs &a, CompSmem<RCH> &sm, int pidx) 
         }
         run_walk<G, RCH>(sm, n, [&](const Run &r, int, int j, bool second) {
             const float jf = (float)j;
-            const float2 w = weight2(e, r, make_float2(jf, jf + 32.0f));
+            const float2 w = weight2<TX, TH>(e, r, make_float2(jf, jf + 32.0f));
             const float2 p = mul2(w, f2(F));
             const float2 pe = fma2(w, f2(Flo), fma2(w, f2(F), make_float2(-p.x, -p.y)));
             const int pix = r.pix0 + j;
@@ -510,6 +532,22 @@ __device__ void render_particle(const DiscArgs &a, CompSmem<RCH> &sm, int pidx) 
         });
         Gp::sync();
     }
+}
+
+// Renders one particle with a group of G threads (a warp or a block).
+template <int G, int RCH>
+__device__ void render_particle(const DiscArgs &a, CompSmem<RCH> &sm, int pidx) {
+    using Gp = Grp<G>;
+    if (Gp::rank() == 0) {
+        disc_setup(a.g, a.theta[pidx], a.phi[pidx], a.ar[pidx], a.flux[pidx], a.cpix[pidx], pidx,
+                   sm.hdr);
+        particle_setup(a.g, sm.hdr, sm.ext, sm.ch);
+    }
+    Gp::sync();
+    const Ext e = sm.ext;
+    with_tiers(e, [&](auto tx, auto th) {
+        render_disc<G, RCH, decltype(tx)::value, decltype(th)::value>(a, sm, e);
+    });
 }
 
 constexpr int kWPB = 8, kRCHW = 64;    // warp kernel
