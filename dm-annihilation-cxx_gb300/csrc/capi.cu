@@ -56,6 +56,7 @@ struct dmann_ctx {
     // workspace
     DevBuf in[7], theta, phi, ar, flux, cpix, key, queue, hist, ctr, fsum, acc, map;
     DevBuf cls, oacc, grad;   // the adjoint's class array, observer sums, staged gradient
+    DevBuf chdr;              // the compensated form's disc headers, one per queue slot
     // halo cores of the ann_core_nosom law (dmann_set_halo_cores)
     DevBuf halo_f, halo_cells, corr;
     HaloGrid halo{};
@@ -277,7 +278,7 @@ void dmann_destroy(dmann_ctx *ctx) {
                       &ctx->theta, &ctx->phi, &ctx->ar, &ctx->flux, &ctx->cpix, &ctx->key,
                       &ctx->queue, &ctx->hist, &ctx->ctr, &ctx->fsum, &ctx->acc, &ctx->map,
                       &ctx->cls, &ctx->oacc, &ctx->grad, &ctx->halo_f, &ctx->halo_cells,
-                      &ctx->corr};
+                      &ctx->corr, &ctx->chdr};
     for (DevBuf *b : bufs)
         if (b->p) cudaFree(b->p);
     for (auto &kv : ctx->rings) {
@@ -611,6 +612,8 @@ dmann_status dmann_map_add_v(dmann_ctx *ctx, const float *x, const float *y, con
         (st = ensure(ctx, ctx->cpix, 4 * N)) || (st = ensure(ctx, ctx->key, 4 * N)) ||
         (st = ensure(ctx, ctx->queue, 4 * N)))
         return st;
+    if (ctx->precision == DMANN_COMP_F32 && (st = ensure(ctx, ctx->chdr, comp_hdr_bytes() * N)))
+        return st;
     // inputs: device pointers are used in place, host arrays are copied
     const float *src[7] = {x, y, z, m, rho, h, law_needs_sigmav(ctx->flux_model) ? sigmav : nullptr};
     const float *dev[7] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
@@ -668,6 +671,7 @@ dmann_status dmann_map_add_v(dmann_ctx *ctx, const float *x, const float *y, con
     da.queue = (const int *)ctx->queue.p;
     da.ctr = pa.ctr;
     da.acc = acc;
+    if (ctx->precision == DMANN_COMP_F32) da.chdr = (CompHdr *)ctx->chdr.p;
     CK(cudaEventRecord(ctx->evd0, s));
     if (ctx->precision == DMANN_PLAIN_F64) CK(launch_disc_plain(da, ctx->num_sms, tu.blocks_per_sm, s, ctx->evdm));
     else CK(launch_disc_comp(da, ctx->num_sms, tu.blocks_per_sm, tu.block_threads, s, ctx->evdm));
@@ -781,6 +785,7 @@ dmann_status issue_observer(dmann_ctx *ctx, const float *const dev[6], int n, in
         da.queue = (const int *)ctx->queue.p;
         da.ctr = pa.ctr;
         da.acc = acc;
+        if (precision == DMANN_COMP_F32) da.chdr = (CompHdr *)ctx->chdr.p;
         if (precision == DMANN_PLAIN_F64) CK(launch_disc_plain(da, ctx->num_sms, tu.blocks_per_sm, s, nullptr));
         else CK(launch_disc_comp(da, ctx->num_sms, tu.blocks_per_sm, tu.block_threads, s, nullptr));
     }
@@ -825,6 +830,8 @@ dmann_status dmann_render_batch(dmann_ctx *ctx, const float *x, const float *y, 
         (st = ensure(ctx, ctx->queue, 4 * n1)) || (st = ensure(ctx, ctx->hist, 4 * (size_t)kKeys)) ||
         (st = ensure(ctx, ctx->ctr, 8 * C_COUNT)) || (st = ensure(ctx, ctx->fsum, 8)) ||
         (st = ensure(ctx, ctx->acc, 8 * Pmax)) || (st = ensure(ctx, ctx->map, 8 * Pmax)))
+        return st;
+    if (precision == DMANN_COMP_F32 && (st = ensure(ctx, ctx->chdr, comp_hdr_bytes() * n1)))
         return st;
     std::vector<RingTables> rts(n_obs);
     for (int k = 0; k < n_obs; k++)
@@ -937,7 +944,9 @@ dmann_status dmann_adjoint(dmann_ctx *ctx, const float *x, const float *y, const
         (st = ensure(ctx, ctx->hist, 4 * (size_t)kKeys)) || (st = ensure(ctx, ctx->ctr, 8 * C_COUNT)) ||
         (st = ensure(ctx, ctx->fsum, 8)) || (st = ensure(ctx, ctx->oacc, 8 * 12)))
         return st;
-    if (precision == DMANN_COMP_F32 && (st = ensure(ctx, ctx->acc, 4 * P)) != DMANN_OK) return st;
+    if (precision == DMANN_COMP_F32 && ((st = ensure(ctx, ctx->acc, 4 * P)) ||
+                                        (st = ensure(ctx, ctx->chdr, comp_hdr_bytes() * n1))))
+        return st;
     const float *src[6] = {x, y, z, m, rho, h};
     const float *dev[6];
     for (int k = 0; k < 6; k++) {
@@ -999,6 +1008,7 @@ dmann_status dmann_adjoint(dmann_ctx *ctx, const float *x, const float *y, const
     da.queue = (const int *)ctx->queue.p;
     da.ctr = pa.ctr;
     da.acc = pa.acc;
+    if (precision == DMANN_COMP_F32) da.chdr = (CompHdr *)ctx->chdr.p;
     CK(cudaEventRecord(ctx->evd0, s));
     CK(launch_adjoint(da, pa.p, pa.out.cls, dgmap, (float *)ctx->acc.p, dgrad, (double *)ctx->oacc.p,
                       precision, ctx->num_sms, s));

@@ -54,11 +54,50 @@ __device__ __forceinline__ float ex2_approx(float x) {
 // packed FP32x2 arithmetic (round to nearest per element)
 __device__ __forceinline__ float2 f2(float v) { return make_float2(v, v); }
 __device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
-__device__ __forceinline__ float2 sub2(float2 a, float2 b) {
-    return __fadd2_rn(a, make_float2(-b.x, -b.y));
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) {   // one packed subtract
+    unsigned long long ua = *reinterpret_cast<unsigned long long *>(&a);
+    unsigned long long ub = *reinterpret_cast<unsigned long long *>(&b);
+    unsigned long long ud;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(ud) : "l"(ua), "l"(ub));
+    return *reinterpret_cast<float2 *>(&ud);
 }
 __device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
 __device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+
+// a + b = s + err exactly (Knuth's TwoSum)
+__device__ __forceinline__ float two_sum(float a, float b, float &err) {
+    const float s = a + b;
+    const float bb = s - a;
+    err = (a - (s - bb)) + (b - bb);
+    return s;
+}
+
+// Two-float sum (s, c) over the warp; every lane ends with the total.
+__device__ __forceinline__ void warp_sum_ff(float &s, float &c) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const float s2 = __shfl_xor_sync(0xffffffffu, s, o);
+        const float c2 = __shfl_xor_sync(0xffffffffu, c, o);
+        float err;
+        s = two_sum(s, s2, err);
+        c = (c + c2) + err;
+    }
+}
+
+// (ah + al) / (bh + bl) as a normalised two-float (Dekker): q1 = ah / bh,
+// the remainder a - q1 b from an exact product (FMA) and an exact
+// difference (q1 bh is within a few ulp of ah), then one correction.
+__device__ inline float2 div_ff(float ah, float al, float bh, float bl) {
+    const float b = bh + bl;
+    const float b_lo = bl - (b - bh);
+    const float q1 = __fdiv_rn(ah, b);
+    const float p = q1 * b;
+    const float pe = fmaf(q1, b, -p);
+    const float r = (((ah - p) - pe) + al) - q1 * b_lo;
+    const float q2 = __fdiv_rn(r, b);
+    const float hi = q1 + q2;
+    return make_float2(hi, q2 - (hi - q1));
+}
 
 constexpr float kHalfPiF = 1.57079632679490f;
 
@@ -76,6 +115,7 @@ struct alignas(16) Run {
 struct Ext {
     float nK;           // -K
     int tier_h, tier_x;  // polynomial lengths (0 shortest, 2 general)
+    float fs_hi, fs_lo;  // flux * inv_scale as a two-float (render only)
 };
 
 // Per-particle constants of the FP32 chord test (see chord_fast).
@@ -87,13 +127,26 @@ struct Chord {
     int fast;           // the FP32 test may be used for this particle
 };
 
-template <int RCH>
-struct CompSmem {
-    Run run[2 * RCH];   // two runs per ring (the second only where it wraps)
+}  // namespace
+
+// Everything the disc kernels need of one particle besides its runs (the
+// type that DiscArgs::chdr points to).
+struct CompHdr {
     DiscHdr hdr;
     Ext ext;
     Chord ch;
+};
+static_assert(sizeof(CompHdr) % 8 == 0, "CompHdr is copied in 8-byte words");
+
+namespace {
+
+template <int RCH>
+struct CompSmem {
+    Run run[2 * RCH];   // two runs per ring (the second only where it wraps)
+    CompHdr h;
     double red[32];
+    float2 red2[32];    // per-warp two-float sums
+    float2 fq;          // flux / S as a two-float
     int cnt_red[32];
     int next_run;       // runs claimed so far in the current pass (block groups)
 };
@@ -382,13 +435,13 @@ __device__ inline int build_runs(const DiscArgs &a, CompSmem<RCH> &sm, int r0, i
                                  AdjRing *aring = nullptr) {
     using Gp = Grp<G>;
     int c = 0;
-    const bool need_a2 = sm.ext.tier_h == 2;
+    const bool need_a2 = sm.h.ext.tier_h == 2;
     for (int i = Gp::rank(); i < n; i += G) {
-        c += make_runs(a, sm.hdr, sm.ch, need_a2, r0 + i, &sm.run[2 * i]);
+        c += make_runs(a, sm.h.hdr, sm.h.ch, need_a2, r0 + i, &sm.run[2 * i]);
         if (aring) {
             const float st = a.rt.st32[r0 + i];
-            aring[i].sr = sinf((float)(a.rt.theta[r0 + i] - sm.hdr.theta0));
-            aring[i].cr = 2.0f * (float)sm.hdr.z0 * st;
+            aring[i].sr = sinf((float)(a.rt.theta[r0 + i] - sm.h.hdr.theta0));
+            aring[i].cr = 2.0f * (float)sm.h.hdr.z0 * st;
             aring[i].st2 = 2.0f * st;
         }
     }
@@ -443,7 +496,7 @@ template <int G, int RCH, int TX, int TH>
 __device__ void render_disc(const DiscArgs &a, CompSmem<RCH> &sm, const Ext &e) {
     using Gp = Grp<G>;
     const int rk = Gp::rank();
-    const int r_first = sm.hdr.r_first, r_last = sm.hdr.r_last;
+    const int r_first = sm.h.hdr.r_first, r_last = sm.h.hdr.r_last;
     const int nring = r_last - r_first + 1;
     const int nchunk = nring > 0 ? (nring + RCH - 1) / RCH : 0;
 
@@ -453,7 +506,7 @@ __device__ void render_disc(const DiscArgs &a, CompSmem<RCH> &sm, const Ext &e) 
     // exactly; the errors are summed apart (not fed back into the next addend,
     // where Kahan's subtraction would round them away again).  The result is
     // independent of the order in which lanes meet the weights to ~1e-12.
-    // The offset is removed in FP64.
+    // The offset is removed exactly after the pass.
     float2 ks = f2(1.0f), kc = f2(0.0f);
     long long total = 0;
     for (int c = 0; c < nchunk; c++) {
@@ -474,32 +527,48 @@ __device__ void render_disc(const DiscArgs &a, CompSmem<RCH> &sm, const Ext &e) 
         });
         Gp::sync();
     }
-    double part = (((double)ks.x - 1.0) + (double)kc.x) + (((double)ks.y - 1.0) + (double)kc.y);
-    part = warp_sum(part);
-    double S = part;
-    if (G > 32) {
-        if ((rk & 31) == 0) sm.red[rk >> 5] = part;
-        Gp::sync();
-        S = 0.0;
-        for (int k = 0; k < Gp::kWarps; k++) S += sm.red[k];
-        Gp::sync();
-    }
     if (total < 2) {  // genmap.cpp:125-128: the whole flux into the centre pixel
         if (rk == 0) {
-            const double vs = sm.hdr.flux * a.f.inv_scale;
-            const float vh = (float)vs;
-            const float vl = (float)(vs - (double)vh);
-            deposit2f(a.acc.hi, a.acc.lo, sm.hdr.cpix, vh);
-            if (vl != 0.0f) red_add_f32(a.acc.lo + sm.hdr.cpix, vl);
+            deposit2f(a.acc.hi, a.acc.lo, sm.h.hdr.cpix, e.fs_hi);
+            if (e.fs_lo != 0.0f) red_add_f32(a.acc.lo + sm.h.hdr.cpix, e.fs_lo);
             atomicAdd((unsigned long long *)(a.ctr + C_DEPOSITS), 1ull);
         }
         Gp::sync();
         return;
     }
     if (rk == 0) atomicAdd((unsigned long long *)(a.ctr + C_DEPOSITS), (unsigned long long)total);
-    // flux / norm as a two-float
-    const double Fd = sm.hdr.flux * a.f.inv_scale / S;
-    const float F = (float)Fd, Flo = (float)(Fd - (double)F);
+    // S = sum of the lanes' (ks - 1) + kc, all in FP32 two-floats: ks - 1 is
+    // exact (1 <= ks < 2^24: a multiple of ulp(ks) below ks), the lane and
+    // warp sums are TwoSum trees, and F = flux inv_scale / S is Dekker's
+    // two-float division (relative error ~2^-44).  Every lane of a warp ends
+    // with the same sums (the xor tree adds the same pairs on each).
+    float S_hi, S_lo;
+    {
+        float err;
+        S_hi = two_sum(ks.x - 1.0f, ks.y - 1.0f, err);
+        S_lo = (kc.x + kc.y) + err;
+        warp_sum_ff(S_hi, S_lo);
+    }
+    float F, Flo;
+    if (G > 32) {
+        if ((rk & 31) == 0) sm.red2[rk >> 5] = make_float2(S_hi, S_lo);
+        Gp::sync();
+        if (rk == 0) {
+            for (int k = 1; k < Gp::kWarps; k++) {
+                float err;
+                S_hi = two_sum(S_hi, sm.red2[k].x, err);
+                S_lo = (S_lo + sm.red2[k].y) + err;
+            }
+            sm.fq = div_ff(e.fs_hi, e.fs_lo, S_hi, S_lo);
+        }
+        Gp::sync();
+        F = sm.fq.x;
+        Flo = sm.fq.y;
+    } else {
+        const float2 q = div_ff(e.fs_hi, e.fs_lo, S_hi, S_lo);
+        F = q.x;
+        Flo = q.y;
+    }
     float *const hi = a.acc.hi, *const lo = a.acc.lo;
 
     // pass 2: deposits.  w*F as hi + lo: the product's rounding error (exact,
@@ -517,7 +586,7 @@ __device__ void render_disc(const DiscArgs &a, CompSmem<RCH> &sm, const Ext &e) 
             const float jf = (float)j;
             const float2 w = weight2<TX, TH>(e, r, make_float2(jf, jf + 32.0f));
             const float2 p = mul2(w, f2(F));
-            const float2 pe = fma2(w, f2(Flo), fma2(w, f2(F), make_float2(-p.x, -p.y)));
+            const float2 pn = fma2(w, f2(-F), p);   // p - w F, exact
             const int pix = r.pix0 + j;
             const float a0 = atom_add_f32(hi + pix, p.x);
             const float a1 = second ? atom_add_f32(hi + pix + 32, p.y) : 0.0f;
@@ -526,7 +595,7 @@ __device__ void render_disc(const DiscArgs &a, CompSmem<RCH> &sm, const Ext &e) 
             const float2 s = add2(av, pv);
             const float2 bb = sub2(s, av);
             float2 err = add2(sub2(av, sub2(s, bb)), sub2(pv, bb));
-            err = add2(err, pe);
+            err = fma2(w, f2(Flo), sub2(err, pn));
             red_add_f32(lo + pix, err.x);
             if (second) red_add_f32(lo + pix + 32, err.y);
         });
@@ -534,17 +603,41 @@ __device__ void render_disc(const DiscArgs &a, CompSmem<RCH> &sm, const Ext &e) 
     }
 }
 
-// Renders one particle with a group of G threads (a warp or a block).
-template <int G, int RCH>
-__device__ void render_particle(const DiscArgs &a, CompSmem<RCH> &sm, int pidx) {
-    using Gp = Grp<G>;
-    if (Gp::rank() == 0) {
-        disc_setup(a.g, a.theta[pidx], a.phi[pidx], a.ar[pidx], a.flux[pidx], a.cpix[pidx], pidx,
-                   sm.hdr);
-        particle_setup(a.g, sm.hdr, sm.ext, sm.ch);
+// The set-up of disc particle pidx: the FP64 geometry of query_disc and
+// the run engine's per-particle constants.
+__device__ inline void setup_hdr(const DiscArgs &a, int pidx, CompHdr &h) {
+    disc_setup(a.g, a.theta[pidx], a.phi[pidx], a.ar[pidx], a.flux[pidx], a.cpix[pidx], pidx, h.hdr);
+    particle_setup(a.g, h.hdr, h.ext, h.ch);
+    const double fs = h.hdr.flux * a.f.inv_scale;
+    h.ext.fs_hi = (float)fs;
+    h.ext.fs_lo = (float)(fs - (double)h.ext.fs_hi);
+}
+
+// Stages the header of queue slot q in shared memory (all threads of the
+// group call this, then synchronise): a copy of the precomputed header when
+// the caller provided them (k_comp_hdr), else the set-up on one thread.
+template <int G>
+__device__ __forceinline__ void stage_hdr(const DiscArgs &a, long long q, CompHdr &dst) {
+    constexpr int kWords = sizeof(CompHdr) / 8;
+    static_assert(kWords <= G, "one word per thread");
+    const int rk = Grp<G>::rank();
+    if (a.chdr) {
+        if (rk < kWords)
+            reinterpret_cast<long long *>(&dst)[rk] =
+                __ldg(reinterpret_cast<const long long *>(a.chdr + q) + rk);
+    } else if (rk == 0) {
+        setup_hdr(a, a.queue[q], dst);
     }
+}
+
+// Renders the particle of queue slot q with a group of G threads (a warp or
+// a block).
+template <int G, int RCH>
+__device__ void render_particle(const DiscArgs &a, CompSmem<RCH> &sm, long long q) {
+    using Gp = Grp<G>;
+    stage_hdr<G>(a, q, sm.h);
     Gp::sync();
-    const Ext e = sm.ext;
+    const Ext e = sm.h.ext;
     with_tiers(e, [&](auto tx, auto th) {
         render_disc<G, RCH, decltype(tx)::value, decltype(th)::value>(a, sm, e);
     });
@@ -568,7 +661,7 @@ __global__ void __launch_bounds__(BT, MINB) k_comp_block(DiscArgs a) {
         const int q = s_q;
         __syncthreads();
         if (q >= nblk) break;
-        render_particle<BT, RCH>(a, sm, a.queue[q]);
+        render_particle<BT, RCH>(a, sm, q);
     }
 }
 
@@ -580,7 +673,7 @@ __global__ void __launch_bounds__(kWPB * 32) k_comp_warp(DiscArgs a) {
     const int w = threadIdx.x >> 5;
     const long long gw = (long long)blockIdx.x * kWPB + w;
     const long long nw = (long long)gridDim.x * kWPB;
-    for (long long q = nblk + gw; q < ndisc; q += nw) render_particle<32, kRCHW>(a, sm[w], a.queue[q]);
+    for (long long q = nblk + gw; q < ndisc; q += nw) render_particle<32, kRCHW>(a, sm[w], q);
 }
 
 template <int BT, int RCH, int MINB>
@@ -621,18 +714,15 @@ __device__ __forceinline__ void kahan(float &s, float &c, float v) {
 }
 
 template <int G, int RCH>
-__device__ void adjc_particle(const adj::AdjArgs &a, AdjcSmem<RCH> &sm, int pidx, double acc[12]) {
+__device__ void adjc_particle(const adj::AdjArgs &a, AdjcSmem<RCH> &sm, long long q, double acc[12]) {
     using Gp = Grp<G>;
     const DiscArgs &da = a.d;
     const int rk = Gp::rank();
-    if (rk == 0) {
-        disc_setup(da.g, da.theta[pidx], da.phi[pidx], da.ar[pidx], da.flux[pidx], da.cpix[pidx],
-                   pidx, sm.c.hdr);
-        particle_setup(da.g, sm.c.hdr, sm.c.ext, sm.c.ch);
-    }
+    stage_hdr<G>(da, q, sm.c.h);
     Gp::sync();
-    const Ext e = sm.c.ext;
-    const int r_first = sm.c.hdr.r_first, r_last = sm.c.hdr.r_last;
+    const int pidx = sm.c.h.hdr.pidx;
+    const Ext e = sm.c.h.ext;
+    const int r_first = sm.c.h.hdr.r_first, r_last = sm.c.h.hdr.r_last;
     const int nring = r_last - r_first + 1;
     const int nchunk = nring > 0 ? (nring + RCH - 1) / RCH : 0;
     const float *g32 = a.gmap32;
@@ -668,7 +758,7 @@ __device__ void adjc_particle(const adj::AdjArgs &a, AdjcSmem<RCH> &sm, int pidx
     if (total < 2) {  // genmap.cpp:125-128: the whole flux in the centre pixel
         if (rk == 0) {
             const double KV[3] = {0.0, 0.0, 0.0};
-            adj::write_grad(a, pidx, a.gmap[sm.c.hdr.cpix] * a.inv_dOmega, 0.0, KV, false, acc);
+            adj::write_grad(a, pidx, a.gmap[sm.c.h.hdr.cpix] * a.inv_dOmega, 0.0, KV, false, acc);
             atomicAdd((unsigned long long *)(da.ctr + C_DEPOSITS), 1ull);
         }
         Gp::sync();
@@ -722,7 +812,7 @@ __device__ void adjc_particle(const adj::AdjArgs &a, AdjcSmem<RCH> &sm, int pidx
     double s2[3] = {(double)vts - (double)vtc, (double)vps - (double)vpc, (double)ts - (double)tc};
     adj::group_sum<G, 3>(s2, sm.red);
     if (rk == 0) {
-        const DiscHdr &d = sm.c.hdr;
+        const DiscHdr &d = sm.c.h.hdr;
         const double ct = cos(d.theta0), st = sin(d.theta0), cp = cos(d.phi0), sp = sin(d.phi0);
         const double V[3] = {s2[0] * ct * cp - s2[1] * sp, s2[0] * ct * sp + s2[1] * cp, -s2[0] * st};
         const double K = adj::kInvC2 * d.flux / (S * d.ar * d.ar) * a.inv_dOmega;
@@ -744,7 +834,7 @@ __global__ void __launch_bounds__(BT, MINB) k_adjc_block(adj::AdjArgs a) {
         const int q = s_q;
         __syncthreads();
         if (q >= nblk) break;
-        adjc_particle<BT, RCH>(a, sm, a.d.queue[q], acc);
+        adjc_particle<BT, RCH>(a, sm, q, acc);
     }
     if (threadIdx.x == 0) adj::flush_acc(a.oacc, acc);
 }
@@ -759,15 +849,36 @@ __global__ void __launch_bounds__(kWPBA * 32) k_adjc_warp(adj::AdjArgs a) {
     const int w = threadIdx.x >> 5;
     const long long gw = (long long)blockIdx.x * kWPBA + w;
     const long long nw = (long long)gridDim.x * kWPBA;
-    for (long long q = nblk + gw; q < ndisc; q += nw) adjc_particle<32, kRCHW>(a, sm[w], a.d.queue[q], acc);
+    for (long long q = nblk + gw; q < ndisc; q += nw) adjc_particle<32, kRCHW>(a, sm[w], q, acc);
     if ((threadIdx.x & 31) == 0) adj::flush_acc(a.oacc, acc);
+}
+
+// The headers of every disc in the queue, one thread per particle (the
+// FP64 set-up at full warp width instead of on one lane of a waiting block).
+__global__ void __launch_bounds__(256) k_comp_hdr(DiscArgs a) {
+    const long long ndisc = a.ctr[C_ADD_DISC];
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < ndisc; q += stride) {
+        CompHdr h;
+        setup_hdr(a, a.queue[q], h);
+        a.chdr[q] = h;
+    }
+}
+
+cudaError_t launch_hdr(const DiscArgs &a, int num_sms, cudaStream_t s) {
+    if (!a.chdr) return cudaSuccess;
+    k_comp_hdr<<<num_sms * 8, 256, 0, s>>>(a);
+    return cudaGetLastError();
 }
 
 }  // namespace
 
+size_t comp_hdr_bytes() { return sizeof(CompHdr); }
+
 cudaError_t launch_disc_comp(const DiscArgs &a, int num_sms, int blocks_per_sm, int block_threads,
                              cudaStream_t s, cudaEvent_t mid) {
-    cudaError_t e;
+    cudaError_t e = launch_hdr(a, num_sms, s);
+    if (e != cudaSuccess) return e;
     if (block_threads == 128) e = launch_block<128, 192, 16>(a, num_sms, blocks_per_sm, s);
     else if (block_threads == 512) e = launch_block<512, 640, 4>(a, num_sms, blocks_per_sm, s);
     else e = launch_block<256, 384, 8>(a, num_sms, blocks_per_sm, s);
@@ -783,8 +894,10 @@ cudaError_t launch_disc_comp(const DiscArgs &a, int num_sms, int blocks_per_sm, 
 
 // The compensated adjoint's disc kernels (block class, then warp class).
 cudaError_t launch_adjoint_comp_discs(const adj::AdjArgs &a, int num_sms, cudaStream_t s) {
+    cudaError_t e = launch_hdr(a.d, num_sms, s);
+    if (e != cudaSuccess) return e;
     int occ = 0;
-    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_adjc_block<256, 256, 4>, 256, 0);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_adjc_block<256, 256, 4>, 256, 0);
     if (e != cudaSuccess) return e;
     if (occ < 1) occ = 1;
     k_adjc_block<256, 256, 4><<<num_sms * occ, 256, 0, s>>>(a);

@@ -72,6 +72,8 @@ struct PrepArgs {
     const double *core_corr;    // per-particle halo-core factor r (ann_core_nosom law)
 };
 
+struct CompHdr;   // the compensated form's per-particle disc header (disc_comp.cu)
+
 struct DiscArgs {
     Hpx g;
     Frame f;
@@ -81,6 +83,9 @@ struct DiscArgs {
     const int *queue;           // disc particles, largest first
     long long *ctr;
     Accum acc;
+    // compensated form: comp_hdr_bytes() per queue slot, filled by the disc
+    // launch; null computes each header inside the disc kernels instead
+    CompHdr *chdr = nullptr;
 };
 
 // prep.cu
@@ -100,6 +105,7 @@ cudaError_t launch_disc_plain(const DiscArgs &a, int num_sms, int blocks_per_sm,
 // anything else means 256).
 cudaError_t launch_disc_comp(const DiscArgs &a, int num_sms, int blocks_per_sm, int block_threads,
                              cudaStream_t s, cudaEvent_t mid);
+size_t comp_hdr_bytes();
 // adjoint.cu: gradients of the plain-form map for dL/dmap = gmap; grad is
 // [6][n] (x, y, z, m, rho, h); oacc[12] (zeroed by the caller) receives
 // sum_i dL/du_i and dL/drot (row-major).  Needs the prep outputs (with cls)
