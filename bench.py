@@ -293,12 +293,16 @@ def run_gb300(args, ws, rank, local):
                        "particles": n, "nside": nside,
                        "form": "compensated FP32 (FP64 geometry, FP32 weights, two-float sums)",
                        "parallelism": f"replicas x{ws}",
-                       "l2": "no flush: inputs 403 MB + map/planes 805 MB > 126 MB L2",
+                       "l2": f"no flush: inputs {24 * n / 1e6:.0f} MB + map/planes "
+                             f"{16 * npix / 1e6:.0f} MB > 126 MB L2",
                        "tuning": dict(tuned["best"], autotune_s=round(tuned["seconds"], 2),
                                       cached=tuned["cached"])},
             "clocks": clocks, "gpu_launches": KERNELS_PER_STEP * args.steps,
             "deposits_per_step": step_stats["deposits"],
             "deposits_per_s": step_stats["deposits"] / (ms / 1e3),
+            # the map's total (sum x dOmega) against the kept particles' flux
+            "flux_conservation_rel": abs(float(comp_map.sum()) * (4 * math.pi / npix) - step_stats["total_flux"])
+                                     / step_stats["total_flux"],
             "stage_ms": {"step": ms, "disc_kernels": statistics.mean(disc_ms),
                          "disc_block": step_stats["disc_block_ms"], "disc_warp": step_stats["disc_warp_ms"],
                          "per_step": [round(x, 2) for x in step_ms]}}
@@ -312,7 +316,9 @@ def run_gb300(args, ws, rank, local):
     traffic = profile_traffic()
     line["roofline"] = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                         "frac": achieved / peak, "peak_source": peak_src,
-                        "traffic": traffic["dram_bytes_per_launch_scaled"] if traffic else None,
+                        # the captured launch's DRAM bytes per deposit (ncu, 2M-particle
+                        # prefix) times this launch's deposits
+                        "traffic": traffic["dram_bytes_per_deposit"] * step_stats["deposits"] if traffic else None,
                         "algorithmic_bytes": alg_bytes,
                         "basis": "8 B per deposit (FP64 map read-modify-write) / disc-kernel time"}
     # the deposit scatter against the L2 reduction rates measured here
