@@ -551,10 +551,7 @@ bool law_needs_sigmav(int model) {
 
 Accum make_accum(dmann_ctx *ctx) {
     Accum acc;
-    const size_t P = (size_t)ctx->g.npix;
     acc.acc64 = (double *)ctx->acc.p;
-    acc.hi = (float *)ctx->acc.p;
-    acc.lo = (float *)ctx->acc.p + P;
     return acc;
 }
 
@@ -988,7 +985,7 @@ dmann_status dmann_adjoint(dmann_ctx *ctx, const float *x, const float *y, const
     pa.hist = (int *)ctx->hist.p;
     pa.ctr = (long long *)ctx->ctr.p;
     pa.flux_sum = (double *)ctx->fsum.p;
-    pa.acc = Accum{nullptr, nullptr, nullptr};
+    pa.acc = Accum{nullptr};
     pa.precision = DMANN_PLAIN_F64;
     pa.block_bucket_min = bmin;
     pa.deposit_singles = 0;

@@ -15,10 +15,13 @@
 // particle's antipode, where asin(sqrt(h)) would lose precision.
 //
 // Normalisation: a compensated FP32 sum per thread (offset so that Fast2Sum
-// captures every rounding error exactly), reduced in FP64.
-// Deposits: two FP32 planes (hi, lo); the hi atomic returns the old value, so
-// the exact TwoSum error of each addition -- plus the product's own rounding
-// error and the low part of flux/norm -- goes to the lo plane.
+// captures every rounding error exactly), reduced as two-floats; flux/norm
+// as a two-float (F, Flo).
+// Deposits: w (F + Flo) rounded once to FP32 (an FMA), converted exactly to
+// FP64 and added with a non-returning red.global.add.f64 into the FP64 plane.
+// Each deposit's only error is that one rounding (relative 2^-24, unbiased),
+// so a particle's deposits add up to its flux to ~2^-24 / sqrt(#pixels) and a
+// pixel's sum of many deposits is far more accurate than each weight.
 //
 // Work layout ("run engine"): the disc's rings are staged in shared memory
 // as runs -- one ring's in-disc pixels, split where the ring wraps so that a
@@ -425,6 +428,17 @@ __device__ __forceinline__ float2 weight2(const Ext &e, const Run &r, float2 jj)
     }
 }
 
+// The double of a float f >= 0 from its bit pattern, with integer operations
+// only (a cvt would run on the FP64 pipe, which GB300 has little of): the
+// exponent is rebiased (127 -> 1023) and the mantissa shifted in.  Exact for
+// normal f; a subnormal or zero f (below 2^-126) becomes a value in
+// [2^-127, 2^-126), so callers do not pass zeros.  sgn (0 or 0x80000000) is
+// the sign of the result.
+__device__ __forceinline__ double f32_to_f64(float f, unsigned sgn) {
+    const unsigned u = __float_as_uint(f);
+    return __hiloint2double((int)(((u >> 3) + (896u << 20)) | sgn), (int)(u << 29));
+}
+
 // Calls f(integral_constant<TX>, integral_constant<TH>) with the particle's
 // tiers as constants where both are below 2 (the common small discs), else
 // with -1 (tiers read at run time): five instantiations of f instead of nine.
@@ -562,8 +576,7 @@ __device__ void render_disc(const DiscArgs &a, CompSmem<RCH> &sm, const Ext &e) 
     }
     if (total < 2) {  // genmap.cpp:125-128: the whole flux into the centre pixel
         if (rk == 0) {
-            deposit2f(a.acc.hi, a.acc.lo, sm.h.hdr.cpix, e.fs_hi);
-            if (e.fs_lo != 0.0f) red_add_f32(a.acc.lo + sm.h.hdr.cpix, e.fs_lo);
+            red_add_f64(a.acc.acc64 + sm.h.hdr.cpix, (double)e.fs_hi + (double)e.fs_lo);
             atomicAdd((unsigned long long *)(a.ctr + C_DEPOSITS), 1ull);
         }
         Gp::sync();
@@ -602,11 +615,16 @@ __device__ void render_disc(const DiscArgs &a, CompSmem<RCH> &sm, const Ext &e) 
         F = q.x;
         Flo = q.y;
     }
-    float *const hi = a.acc.hi, *const lo = a.acc.lo;
+    // |F| and the sign apart: the products are then >= 0 for the exact
+    // conversion to FP64 (f32_to_f64), and the sign goes into its bit.  The
+    // weights are >= exp(-6) (the disc edge), so a product is zero only when
+    // the flux is: such a particle deposits nothing.
+    if (F == 0.0f && Flo == 0.0f) return;
+    const unsigned sgn = F < 0.0f ? 0x80000000u : 0u;
+    const float Fa = fabsf(F), Floa = F < 0.0f ? -Flo : Flo;
+    double *const acc = a.acc.acc64;
 
-    // pass 2: deposits.  w*F as hi + lo: the product's rounding error (exact,
-    // from an FMA) and w*Flo go to the lo plane with the TwoSum error of the
-    // hi atomic, so a particle's deposits add up to its flux to ~1e-12.
+    // pass 2: deposits, one FP64 reduction per pixel (see the file header).
     for (int c = 0; c < nchunk; c++) {
         const int r0 = r_first + c * RCH;
         const int n = min(RCH, r_last - r0 + 1);
@@ -618,19 +636,10 @@ __device__ void render_disc(const DiscArgs &a, CompSmem<RCH> &sm, const Ext &e) 
         run_walk<G, RCH>(sm, n, [&](const Run &r, int, int j, bool second) {
             const float jf = (float)j;
             const float2 w = weight2<TX, TH>(e, r, make_float2(jf, jf + 32.0f));
-            const float2 p = mul2(w, f2(F));
-            const float2 pn = fma2(w, f2(-F), p);   // p - w F, exact
-            const int pix = r.pix0 + j;
-            const float a0 = atom_add_f32(hi + pix, p.x);
-            const float a1 = second ? atom_add_f32(hi + pix + 32, p.y) : 0.0f;
-            const float2 av = make_float2(a0, a1);
-            const float2 pv = p;   // the y half's error is unused where !second
-            const float2 s = add2(av, pv);
-            const float2 bb = sub2(s, av);
-            float2 err = add2(sub2(av, sub2(s, bb)), sub2(pv, bb));
-            err = fma2(w, f2(Flo), sub2(err, pn));
-            red_add_f32(lo + pix, err.x);
-            if (second) red_add_f32(lo + pix + 32, err.y);
+            const float2 p = fma2(w, f2(Fa), mul2(w, f2(Floa)));   // w |F|, rounded once
+            double *const m = acc + (r.pix0 + j);
+            red_add_f64(m, f32_to_f64(p.x, sgn));
+            if (second) red_add_f64(m + 32, f32_to_f64(p.y, sgn));
         });
         Gp::sync();
     }

@@ -43,9 +43,11 @@ struct PrepOut {
 // Particle classes written to PrepOut::cls.
 enum PClass : signed char { PC_SKIPPED = 0, PC_INVALID = 1, PC_SINGLE = 2, PC_DISC = 3 };
 
+// The accumulation plane: per pixel an FP64 sum.  The plain form adds the
+// flux itself; the compensated form adds flux * inv_scale (its FP32
+// products stay normal), which the final pass multiplies back.
 struct Accum {
-    double *acc64;      // DMANN_PLAIN_F64
-    float *hi, *lo;     // DMANN_COMP_F32 (compensated two-float planes)
+    double *acc64;
 };
 
 // Halo cores of the ann_core_nosom law, bucketed into a uniform grid whose

@@ -197,8 +197,7 @@ extern "C" dmann_status dmann_render_noalloc(const float *x, const float *y, con
 
     Accum acc;
     acc.acc64 = nullptr;
-    acc.hi = (float *)(b + L.acc);
-    acc.lo = acc.hi + npix;
+    acc.acc64 = (double *)(b + L.acc);
 
     // the array keeps the previous call's contents: clear what must start at zero
     NA_CK(cudaMemsetAsync(b + L.hist, 0, sizeof(int) * (size_t)kKeys, s));

@@ -179,15 +179,9 @@ __global__ void __launch_bounds__(256) k_prep(PrepArgs a) {
         double *acc = a.acc.acc64;
         aggregated_add(single, cpix, flux, [acc](int p, double v) { red_add_f64(acc + p, v); });
     } else {
-        float *hi = a.acc.hi, *lo = a.acc.lo;
+        double *acc = a.acc.acc64;
         const double sc = a.f.inv_scale;
-        aggregated_add(single, cpix, flux, [hi, lo, sc](int p, double v) {
-            double vs = v * sc;
-            float vh = (float)vs;
-            float vl = (float)(vs - (double)vh);
-            deposit2f(hi, lo, p, vh);
-            if (vl != 0.0f) red_add_f32(lo + p, vl);
-        });
+        aggregated_add(single, cpix, flux, [acc, sc](int p, double v) { red_add_f64(acc + p, v * sc); });
     }
     count_warp(a.ctr + C_DEPOSITS, single);
 }
@@ -259,7 +253,7 @@ __global__ void k_finalize(Accum acc, int precision, int npix, double dOmega, do
         if (precision == 0) {
             v = acc.acc64[p] / dOmega;
         } else {
-            v = ((double)acc.hi[p] + (double)acc.lo[p]) * scale / dOmega;
+            v = acc.acc64[p] * scale / dOmega;
         }
         out[p] = accumulate ? out[p] + v : v;
     }
