@@ -9,7 +9,7 @@ reference's simulation data), one observer at 8 kpc, HEALPix Nside 2048.
 A step renders the whole particle set into one map.  ``value`` times steps
 with inputs resident in HBM; ``e2e`` times the public API with pinned host
 inputs and a host map (H2D of the particles and D2H of the 403 MB map inside
-every step).  Inputs (403 MB) plus the map and accumulation planes (805 MB)
+every step).  Inputs (403 MB) plus the map and the accumulation plane (805 MB)
 exceed the 126 MB L2, so no explicit L2 flush is done between steps.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
@@ -160,7 +160,8 @@ def profile_traffic():
 
 def measure_l2_red(device, nbytes=400_000_000):
     """Live L2 reduction rates (operations/s) of the library's own sweep
-    microbenchmark over a 400 MB array: FP32 red and the compensated deposit."""
+    microbenchmark over a 400 MB array: FP64 red (the deposit of both forms),
+    FP32 red and the returning-atomic compensated FP32 deposit."""
     import ctypes as C
     from annmap import _lib
     L = _lib.load()
@@ -328,6 +329,8 @@ def run_gb300(args, ws, rank, local):
         "achieved_ops": dep_rate, "unit": "reductions/s",
         "peak_red_f32_ops": l2["red_f32"], "peak_comp_f32_ops": l2["comp_f32"],
         "peak_red_f64_ops": l2["red_f64"],
+        # each deposit is one red.global.add.f64
+        "frac_red_f64": dep_rate / l2["red_f64"] if l2["red_f64"] else None,
         "frac_red_f32": dep_rate / l2["red_f32"] if l2["red_f32"] else None,
         "frac_comp_f32": dep_rate / l2["comp_f32"] if l2["comp_f32"] else None,
         "basis": "deposits / disc-kernel time vs a coalesced sweep of reductions over 400 MB"}

@@ -2,8 +2,8 @@
 // that may not allocate device memory.
 //
 // Every scratch buffer the render needs (ring tables, the key histogram and
-// counters, the per-particle prep arrays and disc queue, the hi/lo
-// accumulation planes) is carved out of one fixed array defined below.  The
+// counters, the per-particle prep arrays and disc queue, the FP64
+// accumulation plane) is carved out of one fixed array defined below.  The
 // array is created when the library is loaded on a GPU and lives until the
 // process exits; nothing in this file calls cudaMalloc, cudaFree or any other
 // allocating routine.  The kernels are the same ones dmann_render launches.

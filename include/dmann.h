@@ -66,9 +66,9 @@ typedef enum {
      * arithmetic on the GPU. */
     DMANN_PLAIN_F64 = 0,
     /* FP64 per-particle geometry and disc bounds; FP32 weights (haversine
-     * distance, Gaussian); per-particle normalisation and per-pixel
-     * accumulation as compensated two-float (hi + lo) sums; FP64 final
-     * reduction.  The fast form. */
+     * distance, Gaussian); per-particle normalisation as compensated
+     * two-float sums; each deposit w * flux / norm rounded once to FP32 and
+     * accumulated per pixel in FP64.  The fast form. */
     DMANN_COMP_F32 = 1
 } dmann_precision;
 
@@ -203,8 +203,8 @@ dmann_status dmann_render_v(dmann_ctx *ctx, const float *x, const float *y,
  * context's device accumulation planes for one map, every add deposits one
  * chunk of particles into them (inputs host or device), end divides by
  * dOmega into map_out (host or device; accumulate != 0 adds to it).  The
- * compensated planes carry the sum across chunks, so a streamed map equals
- * a single-call one to accumulation rounding. */
+ * FP64 plane carries the sum across chunks, so a streamed map equals a
+ * single-call one to the rounding of the FP64 additions. */
 dmann_status dmann_map_begin(dmann_ctx *ctx, int nside, int precision);
 dmann_status dmann_map_add(dmann_ctx *ctx, const float *x, const float *y,
                            const float *z, const float *m, const float *rho,
