@@ -432,11 +432,15 @@ __device__ __forceinline__ float2 weight2(const Ext &e, const Run &r, float2 jj)
 // only (a cvt would run on the FP64 pipe, which GB300 has little of): the
 // exponent is rebiased (127 -> 1023) and the mantissa shifted in.  Exact for
 // normal f; a subnormal or zero f (below 2^-126) becomes a value in
-// [2^-127, 2^-126), so callers do not pass zeros.  sgn (0 or 0x80000000) is
-// the sign of the result.
-__device__ __forceinline__ double f32_to_f64(float f, unsigned sgn) {
+// [2^-127, 2^-126), so callers do not pass zeros.  bias is f64_bias(sign):
+// the exponent offset with the result's sign bit (u >> 3 stays below 2^28, so
+// adding the bit sets it).
+__host__ __device__ constexpr unsigned f64_bias(bool negative) {
+    return (896u << 20) + (negative ? 0x80000000u : 0u);
+}
+__device__ __forceinline__ double f32_to_f64(float f, unsigned bias) {
     const unsigned u = __float_as_uint(f);
-    return __hiloint2double((int)(((u >> 3) + (896u << 20)) | sgn), (int)(u << 29));
+    return __hiloint2double((int)((u >> 3) + bias), (int)(u << 29));
 }
 
 // Calls f(integral_constant<TX>, integral_constant<TH>) with the particle's
@@ -620,7 +624,7 @@ __device__ void render_disc(const DiscArgs &a, CompSmem<RCH> &sm, const Ext &e) 
     // weights are >= exp(-6) (the disc edge), so a product is zero only when
     // the flux is: such a particle deposits nothing.
     if (F == 0.0f && Flo == 0.0f) return;
-    const unsigned sgn = F < 0.0f ? 0x80000000u : 0u;
+    const unsigned bias = f64_bias(F < 0.0f);
     const float Fa = fabsf(F), Floa = F < 0.0f ? -Flo : Flo;
     double *const acc = a.acc.acc64;
 
@@ -638,8 +642,8 @@ __device__ void render_disc(const DiscArgs &a, CompSmem<RCH> &sm, const Ext &e) 
             const float2 w = weight2<TX, TH>(e, r, make_float2(jf, jf + 32.0f));
             const float2 p = fma2(w, f2(Fa), mul2(w, f2(Floa)));   // w |F|, rounded once
             double *const m = acc + (r.pix0 + j);
-            red_add_f64(m, f32_to_f64(p.x, sgn));
-            if (second) red_add_f64(m + 32, f32_to_f64(p.y, sgn));
+            red_add_f64(m, f32_to_f64(p.x, bias));
+            if (second) red_add_f64(m + 32, f32_to_f64(p.y, bias));
         });
         Gp::sync();
     }

@@ -10,8 +10,9 @@ namespace dmann {
 
 // Sort keys of disc particles: (31 - log2 size bucket) * kCells + sky cell,
 // so the queue runs from the largest discs to the smallest (longest jobs
-// first) and, within a size bucket, in sky order (neighbouring discs are
-// rendered together and share L2 lines of the map).
+// first) and, within a size bucket, in sky order taking turns among 16
+// coarse regions (discs rendered together share L2 lines of the map but
+// spread over 16 places; see morton_cell in prep.cu).
 constexpr int kCellBits = 12;
 constexpr int kCells = 1 << kCellBits;
 constexpr int kBuckets = 32;

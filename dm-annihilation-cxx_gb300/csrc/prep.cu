@@ -15,13 +15,20 @@ namespace {
 constexpr unsigned kFull = 0xffffffffu;
 
 __device__ inline int morton_cell(double theta, double phi) {
-    // 64 x 64 cells in (theta, phi), bits interleaved (Z order)
+    // 64 x 64 cells in (theta, phi), bits interleaved (Z order), with the
+    // top 4 bits (16 coarse sky regions) rotated to the bottom: consecutive
+    // cells of the queue take turns among the 16 regions and keep Z order
+    // within each.  The discs rendered at the same time then spread over 16
+    // regions -- fewer reductions to the same pixel queue up in L2 -- while
+    // each region's discs still share L2 lines (16M particles at Nside 2048:
+    // 4.8 % faster than plain Z order; rotating 2, 3, 5 or 6 bits: 3.5, 4.2,
+    // 4.2, 3.2 %).
     int it = min(63, max(0, (int)(theta * (64.0 / kPi))));
     int ip = min(63, max(0, (int)(phi * (64.0 / kTwoPi))));
     int c = 0;
 #pragma unroll
     for (int b = 0; b < 6; b++) c |= (((it >> b) & 1) << (2 * b + 1)) | (((ip >> b) & 1) << (2 * b));
-    return c;
+    return ((c << 4) | (c >> (kCellBits - 4))) & (kCells - 1);
 }
 
 // Adds `v` at `pix` once per group of lanes that share `pix` (warp
