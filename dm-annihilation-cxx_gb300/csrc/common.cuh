@@ -273,22 +273,6 @@ __device__ inline float atom_add_f32(float *addr, float v) {
     return old;
 }
 
-// Compensated (two-float) accumulation into the hi/lo planes: the atomic
-// returns the old hi value, so the rounding error of old + v (Knuth's
-// TwoSum, exact in round-to-nearest) is known and goes to the lo plane.
-// Valid while the values stay normal floats (the deposits are scaled by a
-// power of two to keep them there).
-// `extra` is a second-order part of the value (e.g. the rounding error of
-// the product that formed v) added to the lo plane with the error.
-__device__ inline void deposit2f(float *hi, float *lo, int pix, float v, float extra = 0.0f) {
-    float a = atom_add_f32(hi + pix, v);
-    float s = __fadd_rn(a, v);
-    float bb = __fsub_rn(s, a);
-    float err = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(v, bb));
-    err = __fadd_rn(err, extra);
-    if (err != 0.0f) red_add_f32(lo + pix, err);
-}
-
 // ---------------------------------------------------------------- reductions
 __device__ inline double warp_sum(double v) {
 #pragma unroll

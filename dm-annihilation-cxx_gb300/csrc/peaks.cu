@@ -9,7 +9,8 @@
 //   DMANN_PEAK_RED_F32   red.global.add.f32 (no return value)
 //   DMANN_PEAK_RED_F64   red.global.add.f64
 //   DMANN_PEAK_RED_U64   red.global.add.u64 (an atomicAdd whose value is unused)
-//   DMANN_PEAK_COMP_F32  the compensated deposit: atom.global.add.f32 that
+//   DMANN_PEAK_COMP_F32  a two-plane compensated FP32 deposit (the disc
+//                        kernels' earlier form): atom.global.add.f32 that
 //                        returns the old value, the exact TwoSum error and a
 //                        red.global.add.f32 of the error into a second plane
 //                        (two planes of bytes/2 each)
@@ -20,6 +21,16 @@
 
 namespace dmann {
 namespace {
+
+// hi[pix] += v with the rounding error (Knuth's TwoSum on the value the
+// atomic returns) added to lo[pix].
+__device__ inline void deposit2f(float *hi, float *lo, int pix, float v) {
+    const float a = atom_add_f32(hi + pix, v);
+    const float s = __fadd_rn(a, v);
+    const float bb = __fsub_rn(s, a);
+    const float err = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(v, bb));
+    if (err != 0.0f) red_add_f32(lo + pix, err);
+}
 
 template <int KIND>
 __global__ void __launch_bounds__(256) k_sweep(void *buf, long long n, int reps, float v) {

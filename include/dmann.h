@@ -292,8 +292,9 @@ dmann_status dmann_render_noalloc(const float *x, const float *y, const float *z
 typedef enum {
     DMANN_PEAK_RED_F32 = 0,   /* red.global.add.f32 */
     DMANN_PEAK_RED_F64 = 1,   /* red.global.add.f64 */
-    DMANN_PEAK_COMP_F32 = 2,  /* the compensated deposit: returning FP32 atomic
-                                 add, exact TwoSum error, FP32 red of the error */
+    DMANN_PEAK_COMP_F32 = 2,  /* a two-plane compensated FP32 deposit: returning
+                                 FP32 atomic add, exact TwoSum error, FP32 red of
+                                 the error */
     DMANN_PEAK_RED_U64 = 3    /* red.global.add.u64 */
 } dmann_peak_kind;
 /* No reference counterpart.  Measures the rate (operations per second) of
