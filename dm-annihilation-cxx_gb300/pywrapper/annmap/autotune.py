@@ -11,6 +11,13 @@ sample) and the one with the least device time wins.  The winner becomes
 the renderer's per-Nside tuning entry (dmann_set_tuning_nside), so later
 renders -- including every observer of a batch with that Nside -- use it.
 
+A prefix sample has the per-particle disc statistics of the whole set but
+not its density: with fewer particles per sky region, fewer concurrently
+rendered discs overlap, fewer reductions to one pixel queue up in L2, and a
+shape that wins on the sample can lose on the whole set (16M particles at
+Nside 2048: 256-thread blocks win on a 2M prefix, 128-thread blocks on the
+whole set).  Tune with ``sample`` equal to the particle count when the
+render is long enough to repay one trial render per candidate.
 Results are cached in a JSON file keyed by device, Nside, precision form
 and the sample size's power of two; ``ANNMAP_TUNING_CACHE`` names the file
 (default ``~/.cache/annmap/tuning.json``), ``cache=False`` disables it.
