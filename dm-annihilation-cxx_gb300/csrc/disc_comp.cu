@@ -392,7 +392,7 @@ __device__ __forceinline__ float2 weight2x(const Ext &e, const Run &r, float2 jj
 // Weights only (the render passes).  For the small-disc tiers the
 // haversine takes sin^2 x as one series in x^2 (sin^2 x = x^2 - x^4/3 +
 // 2x^6/45 - x^8/315 + ..., from (1 - cos 2x)/2): to x^4 for tier 0 and to x^8
-// for tier 1, truncation below 2e-8 relative (|x| < 0.025, resp. 0.33), one
+// for tier 1, truncation below 1.8e-8 resp. 2.1e-8 relative (|x| < 0.025, resp. 0.33), one
 // operation fewer than sin x squared; and -K multiplies the asin^2 series'
 // coefficients instead of its value.
 template <int TX = -1, int TH = -1>
