@@ -258,9 +258,11 @@ def run_gb300(args, ws, rank, local):
     if args.no_tune:
         tuned = {"best": r.get_tuning(), "seconds": 0.0, "cached": False}
     else:
-        # on the whole set: how many discs overlap while rendered (the
-        # density, which a prefix sample lowers) decides the block shape
-        tuned = autotune.tune(r, dparts, nside, annmap.COMP_F32, sample=n, reps=1, out=dmap)
+        # on the whole set up to 16M particles: how many discs overlap while
+        # rendered (the density, which a prefix sample lowers) decides the
+        # block shape; beyond that a 16M prefix keeps tuning within a minute
+        tuned = autotune.tune(r, dparts, nside, annmap.COMP_F32, sample=min(n, 1 << 24), reps=1,
+                              out=dmap)
 
     disc_ms, step_ms, step_stats = [], [], None
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
