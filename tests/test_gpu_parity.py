@@ -156,8 +156,11 @@ def test_streaming_equals_single_call(rend, precision):
     rend.add({k: v[:0] for k, v in d.items()})  # an empty chunk
     two = rend.end()
     # chunking changes only the order of the additions, which both forms make
-    # in FP64 (rounding at ~1e-16 of a pixel)
-    tol = 1e-12
+    # in FP64 (rounding at ~1e-16 of a pixel).  In the compensated form the
+    # order in which warps claim rings also moves a particle's normalisation
+    # by ~1e-13, so a deposit lying that close to an FP32 rounding boundary
+    # rounds the other way: at most 2^-24 of that deposit.
+    tol = 1e-12 if precision == PLAIN else 1e-7
     np.testing.assert_allclose(two, one, rtol=tol, atol=0)
     acc = rend.render(P.as_dict(), nside, precision, out=one.copy(), accumulate=True)
     np.testing.assert_allclose(acc, 2 * one, rtol=tol)
@@ -174,8 +177,9 @@ def test_device_inputs_and_output(rend):
     out = torch.zeros(12 * nside * nside, dtype=torch.float64, device="cuda")
     rend.render(dev, nside, COMP, out=out)
     torch.cuda.synchronize()
-    # same arithmetic; the order of the FP64 reductions differs run to run
-    np.testing.assert_allclose(out.cpu().numpy(), host, rtol=1e-12)
+    # same arithmetic; the order of the FP64 reductions differs run to run,
+    # and a deposit may round the other way in FP32 (see the chunking test)
+    np.testing.assert_allclose(out.cpu().numpy(), host, rtol=1e-7)
 
 
 def test_edge_cases(rend):
