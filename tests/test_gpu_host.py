@@ -43,7 +43,9 @@ def test_cpp_genmap_chunking_is_linear(tmp_path):
     mb, tb = host.genmap(info_b, COMP)
     m = ma > 0
     assert np.array_equal(ma > 0, mb > 0)
-    assert np.max(np.abs(ma[m] - mb[m]) / ma[m]) < 1e-10
+    # FP64 sums in another order; a deposit's one FP32 rounding may flip
+    # where the ring-claim order moved its particle's normalisation by ~1e-13
+    assert np.max(np.abs(ma[m] - mb[m]) / ma[m]) < 1e-7
     assert math.isclose(ta, tb, rel_tol=1e-12)
 
 

@@ -76,7 +76,9 @@ def test_batch_honours_per_nside_tuning(setup):
     par.set_observer(P.obs_pos)
     for b, o in zip(base, outs):
         o = o.cpu().numpy()
-        assert np.array_equal(o != 0, b != 0) and _rel(o, b) < 1e-9
+        # other block shapes claim rings in another order: a deposit's one FP32
+        # rounding may flip (at most 2^-24 of that deposit)
+        assert np.array_equal(o != 0, b != 0) and _rel(o, b) < 1e-7
 
 
 def test_autotune_applies_the_fastest(setup, tmp_path):
