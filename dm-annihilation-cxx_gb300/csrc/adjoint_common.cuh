@@ -3,6 +3,7 @@
 // particle's Gb = dL/dF, K T and K V (see adjoint.cu for the formulas), the
 // gradient with respect to x, y, z, m, rho, h and its observer terms.
 #pragma once
+#include "../../include/dmann.h"
 #include "kernels.cuh"
 
 namespace dmann {
@@ -37,7 +38,10 @@ __device__ inline void write_grad(const AdjArgs &a, int i, double Gb, double KT,
     const double d = particle_u(a, i, u);
     const double inv_d = 1.0 / d;
     const double uh[3] = {u[0] * inv_d, u[1] * inv_d, u[2] * inv_d};
-    const double m = (double)a.p.m[i], rho = (double)a.p.rho[i];
+    // F = fd rho m (nosom), or fd m under the decay law (flux_decay.cpp:9-16,
+    // unit_factor then being its own): there dL/drho = 0
+    const bool decay = a.d.f.flux_model == DMANN_FLUX_DECAY;
+    const double m = (double)a.p.m[i], rho = decay ? 1.0 : (double)a.p.rho[i];
     const double fd = a.d.f.unit_factor / (4.0 * kPi * d * d);   // F / (rho m)
     const double F = fd * rho * m;
     const double w[3] = {-KV[0], -KV[1], KV[2]};                 // D K V
@@ -51,7 +55,7 @@ __device__ inline void write_grad(const AdjArgs &a, int i, double Gb, double KT,
         acc[j] += g;
     }
     a.grad[(size_t)3 * n + i] = Gb * fd * rho;
-    a.grad[(size_t)4 * n + i] = Gb * fd * m;
+    a.grad[(size_t)4 * n + i] = decay ? 0.0 : Gb * fd * m;
     a.grad[(size_t)5 * n + i] = disc ? KT / (double)a.p.h[i] : 0.0;
     if (disc) {
 #pragma unroll

@@ -923,8 +923,8 @@ dmann_status dmann_adjoint(dmann_ctx *ctx, const float *x, const float *y, const
     if (nside < 1 || nside > 8192) return fail(ctx, DMANN_ERR_INVALID, "nside must be in [1, 8192]");
     if (!ctx->have_frame) return fail(ctx, DMANN_ERR_STATE, "observer frame not set");
     if (!ctx->have_units) return fail(ctx, DMANN_ERR_STATE, "units not set");
-    if (ctx->flux_model != DMANN_FLUX_ANN_NOSOM)
-        return fail(ctx, DMANN_ERR_INVALID, "the adjoint supports the nosom flux law only");
+    if (ctx->flux_model != DMANN_FLUX_ANN_NOSOM && ctx->flux_model != DMANN_FLUX_DECAY)
+        return fail(ctx, DMANN_ERR_INVALID, "the adjoint supports the nosom and decay flux laws only");
     dmann_status st = check_particles(ctx, x, y, z, m, rho, h, n);
     if (st != DMANN_OK) return st;
     CK(cudaSetDevice(ctx->device));

@@ -230,7 +230,9 @@ dmann_status dmann_render_batch(dmann_ctx *ctx, const float *x, const float *y,
                                 double *const *maps);
 
 /* ---- differentiation ---- */
-/* Adjoint of dmann_render's plain FP64 form (no reference counterpart).
+/* Adjoint of dmann_render (no reference counterpart), for the nosom and
+ * decay flux laws (their flux is rho m, or m, times a constant over d^2;
+ * under decay dL/drho = 0); other laws give DMANN_ERR_INVALID.
  * grad_map[p] = dL/dmap[p] for a scalar loss L of the map dmann_render
  * returns for these particles, this nside and the context's frame and units
  * (12*nside^2 doubles, host or device).  Writes dL/d(particle inputs) into

@@ -522,6 +522,8 @@ void orc_particle_losses(const orc_params *p, const double *mass, const double *
 int orc_adjoint(const orc_params *p, const float *mass, const float *dens,
                 const float *hsmooth, const float *x, const float *y, const float *z,
                 int64_t n, const double *G, double *grad, double oacc[12]) {
+    /* laws whose flux is rho m (or m) times a constant over d^2 */
+    if (p->flux_model != 0 && p->flux_model != 4) return -2;
     orc_hpx hb;
     orc_hpx_init(&hb, p->nside);
     int32_t *list = (int32_t *)malloc(sizeof(int32_t) * (size_t)p->npix);
@@ -568,8 +570,12 @@ int orc_adjoint(const orc_params *p, const float *mass, const float *dens,
                        (double)z[i] - p->obs_pos[2]};
         double d = g.d;
         double uh[3] = {u[0] / d, u[1] / d, u[2] / d};
-        double fd = p->unit_factor / (4.0 * PI * d * d);
-        double F = fd * (double)dens[i] * (double)mass[i];
+        /* F = fd rho m (nosom), or fd m with the decay law's own unit factor
+           (src/flux/flux_decay.cpp:9-16): then dL/drho = 0 */
+        int decay = p->flux_model == 4;
+        double fd = (decay ? p->decay_unit_factor : p->unit_factor) / (4.0 * PI * d * d);
+        double rho_f = decay ? 1.0 : (double)dens[i];
+        double F = fd * rho_f * (double)mass[i];
         double w[3] = {-KV[0], -KV[1], KV[2]}; /* D K V, D = diag(-1,-1,1) */
         double cr = -(2.0 * Gb * F + KT) / d;
         for (int j = 0; j < 3; j++) {
@@ -579,8 +585,8 @@ int orc_adjoint(const orc_params *p, const float *mass, const float *dens,
             grad[j * n + i] = gj;
             oacc[j] += gj;
         }
-        grad[3 * n + i] = Gb * fd * (double)dens[i];
-        grad[4 * n + i] = Gb * fd * (double)mass[i];
+        grad[3 * n + i] = Gb * fd * rho_f;
+        grad[4 * n + i] = decay ? 0.0 : Gb * fd * (double)mass[i];
         if (npd >= 0) {
             grad[5 * n + i] = KT / (double)hsmooth[i];
             for (int j = 0; j < 3; j++)

@@ -93,3 +93,38 @@ def test_sky_map_rejects_cpu_tensors():
     t = torch.zeros(4)
     with pytest.raises(ValueError):
         sky_map(t, t, t, t, t, t, torch.zeros(3, dtype=torch.float64), nside=4)
+
+
+@pytest.fixture(scope="module")
+def decay_case():
+    """The decay law (src/flux/flux_decay.cpp): flux ~ m / d^2, no rho."""
+    P, parts, p0 = make_case(2000, 128, seed=23, single_frac=0.2, skipped=20)
+    p = O.make_params(nside=128, obs_pos=P.obs_pos, centerpos=P.centerpos, align_vec=P.align_vec,
+                      particle_masses=(P.particle_mass,), flux_model=4)
+    mp, _, _ = O.render(p, parts)
+    target, _, _ = O.render(p, __import__("adjoint_cases").jittered(P))
+    _, G = loss_grad(mp, target)
+    grad, oacc = O.adjoint(p, parts, G)
+    return P, parts, p, G, grad, mp
+
+
+def test_oracle_adjoint_decay_law(decay_case):
+    P, parts, p, G, grad, mp = decay_case
+    assert np.all(grad[4] == 0.0)                      # no rho in the decay flux
+    res = fd_check(p, parts, G, grad)
+    for k in ("x", "y", "z", "m", "h"):
+        err, n_ok = res[k]
+        assert n_ok > 1600, (k, n_ok)
+        assert err < 1e-6, (k, err)
+    L = float(np.dot(G, mp))
+    m = parts["m"].astype(np.float64)
+    assert np.sum(m * grad[3]) == pytest.approx(L, rel=1e-10)
+
+
+def test_oracle_adjoint_rejects_other_laws():
+    P, parts, p0 = make_case(200, 32, seed=3)
+    for law in (1, 2, 3, 5, 6):
+        p = O.make_params(nside=32, obs_pos=P.obs_pos, centerpos=P.centerpos,
+                          align_vec=P.align_vec, particle_masses=(P.particle_mass,), flux_model=law)
+        with pytest.raises(RuntimeError):
+            O.adjoint(p, parts, np.ones(12 * 32 * 32))

@@ -11,6 +11,8 @@ Function over it) against its references.
   * the observer gradient (forward-mode rotation Jacobian on the GPU side,
     finite-difference Jacobian on the oracle side) <= 1e-8 of the oracle's,
     and <= 1e-6 of central differences of the summed loss;
+  * the decay law (flux ~ m / d^2): dL/drho = 0 and the other fields as
+    the oracle's; laws with other dependences are refused;
   * at the full adjoint workload (4,194,304 particles, Nside 512) the
     size-independent Euler identities of the map: it is linear in m and in
     rho, and homogeneous of degree -2 in (pos - opos, h), so
@@ -192,3 +194,40 @@ def test_adjoint_full_workload_euler_identities(prec):
     assert np.sum(m * grad[3]) == pytest.approx(L, rel=tol)
     assert np.sum(rho * grad[4]) == pytest.approx(L, rel=tol)
     assert np.sum(u * grad[:3]) + np.sum(h * grad[5]) == pytest.approx(-2 * L, rel=10 * tol)
+
+
+@pytest.mark.parametrize("prec", [PLAIN, COMP], ids=["plain", "comp"])
+def test_adjoint_decay_law_matches_oracle(prec):
+    """The decay law (flux ~ m / d^2 with its own unit factor): dL/drho = 0,
+    the other fields against the oracle's FP64 adjoint."""
+    P, parts, p0 = make_case(20000, 128, seed=29, single_frac=0.2, skipped=100)
+    p = O.make_params(nside=128, obs_pos=P.obs_pos, centerpos=P.centerpos, align_vec=P.align_vec,
+                      particle_masses=(P.particle_mass,), flux_model=4)
+    r = annmap.Renderer(0)
+    r.set_observer(P.obs_pos, P.centerpos, P.align_vec)
+    r.set_units(p.decay_unit_factor, p.hires_threshold, flux_model=4)
+    mp = r.render(parts, 128, PLAIN)
+    ref_map, _, _ = O.render(p, parts)
+    assert _normwise(mp, ref_map) <= 1e-12
+    target = r.render(jittered(P), 128, PLAIN)
+    _, G = loss_grad(mp, target)
+    grad, gopos = r.adjoint(parts, 128, G, precision=prec)
+    r.close()
+    ref, oacc = O.adjoint(p, parts, G)
+    assert np.all(grad[4] == 0.0)
+    for k, f in enumerate(FIELDS):
+        if f == "rho":
+            continue
+        assert _normwise(grad[k], ref[k]) <= TOL_ORACLE[prec], (f, _normwise(grad[k], ref[k]))
+    go_ref = O.observer_grad(p, oacc)
+    assert np.linalg.norm(gopos - go_ref) <= TOL_OBS[prec] * np.linalg.norm(go_ref)
+
+
+def test_adjoint_rejects_laws_with_other_dependences():
+    P, parts, p = make_case(500, 32, seed=31)
+    r = annmap.Renderer(0)
+    r.set_observer(P.obs_pos, P.centerpos, P.align_vec)
+    r.set_units(p.unit_factor, p.hires_threshold, flux_model=1)   # somv: needs sigma v
+    with pytest.raises(annmap.DmannError):
+        r.adjoint(parts, 32, np.ones(12 * 32 * 32))
+    r.close()
