@@ -22,7 +22,7 @@ from __future__ import annotations
 import numpy as np
 import torch
 
-from ._lib import PLAIN_F64
+from ._lib import FLUX_LAWS, PLAIN_F64
 from .mapgen import Renderer
 
 _RENDERERS: dict = {}
@@ -38,30 +38,30 @@ def _renderer(device: int) -> Renderer:
 class SkyMap(torch.autograd.Function):
     @staticmethod
     def forward(ctx, x, y, z, m, rho, h, opos, nside, cpos, align, unit_factor, hires_threshold,
-                precision):
+                precision, flux_model):
         if not x.is_cuda:
             raise ValueError("sky_map needs CUDA tensors")
         dev = x.device.index if x.device.index is not None else torch.cuda.current_device()
         r = _renderer(dev)
         op = [float(v) for v in opos.detach().to("cpu", torch.float64)]
         r.set_observer(op, cpos, align)
-        r.set_units(unit_factor, hires_threshold)
+        r.set_units(unit_factor, hires_threshold, flux_model)
         parts = {"x": x.detach(), "y": y.detach(), "z": z.detach(), "m": m.detach(),
                  "rho": rho.detach(), "h": h.detach()}
         out = torch.empty(12 * nside * nside, dtype=torch.float64, device=x.device)
         r.render(parts, nside, precision, out=out)
         ctx.save_for_backward(x, y, z, m, rho, h)
         ctx.cfg = (dev, op, tuple(cpos), tuple(align), float(unit_factor), float(hires_threshold),
-                   int(nside), int(precision))
+                   int(nside), int(precision), int(flux_model))
         return out
 
     @staticmethod
     def backward(ctx, grad_map):
         x, y, z, m, rho, h = ctx.saved_tensors
-        dev, op, cpos, align, uf, thr, nside, precision = ctx.cfg
+        dev, op, cpos, align, uf, thr, nside, precision, law = ctx.cfg
         r = _renderer(dev)
         r.set_observer(op, cpos, align)
-        r.set_units(uf, thr)
+        r.set_units(uf, thr, law)
         parts = {"x": x.detach(), "y": y.detach(), "z": z.detach(), "m": m.detach(),
                  "rho": rho.detach(), "h": h.detach()}
         g, gopos = r.adjoint(parts, nside, grad_map.detach().to(torch.float64).contiguous(),
@@ -69,16 +69,21 @@ class SkyMap(torch.autograd.Function):
         grads = [g[k].to(t.dtype) if t.requires_grad else None
                  for k, t in enumerate((x, y, z, m, rho, h))]
         gop = torch.as_tensor(np.asarray(gopos), dtype=torch.float64) if ctx.needs_input_grad[6] else None
-        return (*grads, gop, None, None, None, None, None, None)
+        return (*grads, gop, None, None, None, None, None, None, None)
 
 
 def sky_map(x, y, z, m, rho, h, opos, *, nside: int, cpos=(0.0, 0.0, 0.0), align=(0.0, 0.0, 1.0),
             unit_factor: float = 1.0, hires_threshold: float = float("inf"),
-            precision: int = PLAIN_F64):
+            precision: int = PLAIN_F64, flux_model=0):
     """The map (12 nside^2 float64, flux per steradian) as a differentiable
     function of the particle arrays and the observer position ``opos``
-    (a length-3 float64 CPU tensor; its gradient is returned on the CPU)."""
+    (a length-3 float64 CPU tensor; its gradient is returned on the CPU).
+    ``flux_model``: the nosom law (0, default) or the decay law (4 or
+    "decay", with unit_factor its own); other laws have no adjoint."""
     if not torch.is_tensor(opos):
         opos = torch.as_tensor(opos, dtype=torch.float64)
+    if isinstance(flux_model, str):
+        flux_model = FLUX_LAWS[flux_model]
     return SkyMap.apply(x, y, z, m, rho, h, opos, int(nside), tuple(float(v) for v in cpos),
-                        tuple(float(v) for v in align), unit_factor, hires_threshold, precision)
+                        tuple(float(v) for v in align), unit_factor, hires_threshold, precision,
+                        int(flux_model))

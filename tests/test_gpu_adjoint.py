@@ -231,3 +231,27 @@ def test_adjoint_rejects_laws_with_other_dependences():
     with pytest.raises(annmap.DmannError):
         r.adjoint(parts, 32, np.ones(12 * 32 * 32))
     r.close()
+
+
+def test_sky_map_autograd_decay_law():
+    torch = pytest.importorskip("torch")
+    from annmap.autograd import sky_map
+    P, parts, p0 = make_case(5000, 64, seed=37, single_frac=0.2)
+    p = O.make_params(nside=64, obs_pos=P.obs_pos, centerpos=P.centerpos, align_vec=P.align_vec,
+                      particle_masses=(P.particle_mass,), flux_model=4)
+    t = {k: torch.from_numpy(np.asarray(v)).cuda().requires_grad_(True) for k, v in parts.items()}
+    opos = torch.tensor(P.obs_pos, dtype=torch.float64, requires_grad=True)
+    mp = sky_map(t["x"], t["y"], t["z"], t["m"], t["rho"], t["h"], opos, nside=64,
+                 cpos=P.centerpos, align=P.align_vec, unit_factor=p.decay_unit_factor,
+                 hires_threshold=p.hires_threshold, flux_model="decay")
+    ref_map, _, _ = O.render(p, parts)
+    assert _normwise(mp.detach().cpu().numpy(), ref_map) <= 1e-12
+    G = np.random.default_rng(2).standard_normal(12 * 64 * 64)
+    (torch.from_numpy(G).cuda() * mp).sum().backward()
+    ref, _ = O.adjoint(p, parts, G)
+    assert np.all(t["rho"].grad.cpu().numpy() == 0.0)
+    for k, f in enumerate(FIELDS):
+        if f == "rho":
+            continue
+        got = t[f].grad.cpu().numpy().astype(np.float64)
+        assert _normwise(got, ref[k]) <= 1e-6, f   # float32 gradients of FP64 values
