@@ -240,9 +240,12 @@ class Parameters:
         self.map.setNside(nside)
 
     # ------------------------------------------------------------------ derived
-    def flux_unit_factor(self, flux_model: int = 0) -> float:
-        """The unit factor of a flux law (dmann_flux_unit_factor): the
-        annihilation laws share unit_factor, the decay law has its own."""
+    def flux_unit_factor(self, flux_model=0) -> float:
+        """The unit factor of a flux law (dmann_flux_unit_factor; a number
+        or a name of _lib.FLUX_LAWS): the annihilation laws share
+        unit_factor, the decay law has its own."""
+        if isinstance(flux_model, str):
+            flux_model = _lib.FLUX_LAWS[flux_model]
         if flux_model == 0:
             return self.unit_factor
         L = _lib.load()

@@ -178,7 +178,8 @@ def test_flux_unit_factors_match_oracle():
     p = O.make_params(nside=8, obs_pos=(1, 2, 3), centerpos=(0, 0, 0), align_vec=(0, 0, 1),
                       particle_masses=(4.1e3,))
     par = annmap.Parameters(text=case["info_text"].replace("@DIR@", "/x"))
-    assert par.flux_unit_factor(4) == p.decay_unit_factor
+    assert par.flux_unit_factor(4) == p.decay_unit_factor == par.flux_unit_factor("decay")
+    assert par.flux_unit_factor("ann_nosom") == par.unit_factor
     for law in (0, 1, 2, 3, 5):
         assert par.flux_unit_factor(law) == p.unit_factor == par.unit_factor
     with pytest.raises(ValueError):
