@@ -28,7 +28,7 @@
 // run is contiguous in the map -- and each warp takes whole runs.  A lane
 // evaluates two pixels of a run at once (j and j + 32) with the packed FP32x2
 // instructions of sm_100+ (__ffma2_rn & co.), halving the issue slots of the
-// polynomial, Kahan and TwoSum arithmetic.
+// polynomials, the compensated sums and the products.
 //
 // Polynomials (written from their Taylor series), the number of terms chosen
 // per particle from the largest |x| and h its disc can reach:
@@ -694,7 +694,7 @@ constexpr int kWPB = 8, kRCHW = 64;    // warp kernel
 // One block per large disc, persistent over the block-class queue (largest
 // discs first, claimed dynamically).  Block shapes: BT threads, runs of RCH
 // rings staged per chunk, MINB resident blocks per SM -- every shape fills
-// the SM with 2048 threads (the kernel is latency bound: returned atomics)
+// the SM with 2048 threads (fewer, with more registers each, measured slower)
 // and about 200 KB of staged runs.  The autotuner picks the shape.
 template <int BT, int RCH, int MINB>
 __global__ void __launch_bounds__(BT, MINB) k_comp_block(DiscArgs a) {
