@@ -102,6 +102,31 @@ int block_bucket_min(const dmann_tuning &t) {
                         std::string(#call) + ": " + cudaGetErrorString(e_));                      \
     } while (0)
 
+// The compensated kernels' disc headers for n particles (comp_hdr_bytes()
+// each, with headroom for slowly growing chunks).  Optional: without them
+// the kernels compute each header themselves -- slower, the same results --
+// so a failed allocation is not an error.
+void reserve_headers(dmann_ctx *ctx, size_t n) {
+    const size_t bytes = comp_hdr_bytes() * (n > 0 ? n : 1);
+    if (ctx->chdr.bytes >= bytes) return;
+    if (ctx->chdr.p) cudaFree(ctx->chdr.p);
+    ctx->chdr.p = nullptr;
+    ctx->chdr.bytes = 0;
+    for (size_t want : {bytes + bytes / 8, bytes}) {
+        if (cudaMalloc(&ctx->chdr.p, want) == cudaSuccess) {
+            ctx->chdr.bytes = want;
+            return;
+        }
+        cudaGetLastError();
+        ctx->chdr.p = nullptr;
+    }
+}
+
+CompHdr *headers_for(const dmann_ctx *ctx, size_t n) {
+    const bool fits = ctx->chdr.p && ctx->chdr.bytes >= comp_hdr_bytes() * (n > 0 ? n : 1);
+    return fits ? (CompHdr *)ctx->chdr.p : nullptr;
+}
+
 dmann_status ensure(dmann_ctx *ctx, DevBuf &b, size_t bytes) {
     if (b.bytes >= bytes) return DMANN_OK;
     if (b.p) {
@@ -609,8 +634,7 @@ dmann_status dmann_map_add_v(dmann_ctx *ctx, const float *x, const float *y, con
         (st = ensure(ctx, ctx->cpix, 4 * N)) || (st = ensure(ctx, ctx->key, 4 * N)) ||
         (st = ensure(ctx, ctx->queue, 4 * N)))
         return st;
-    if (ctx->precision == DMANN_COMP_F32 && (st = ensure(ctx, ctx->chdr, comp_hdr_bytes() * N)))
-        return st;
+    if (ctx->precision == DMANN_COMP_F32) reserve_headers(ctx, N);
     // inputs: device pointers are used in place, host arrays are copied
     const float *src[7] = {x, y, z, m, rho, h, law_needs_sigmav(ctx->flux_model) ? sigmav : nullptr};
     const float *dev[7] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
@@ -668,7 +692,7 @@ dmann_status dmann_map_add_v(dmann_ctx *ctx, const float *x, const float *y, con
     da.queue = (const int *)ctx->queue.p;
     da.ctr = pa.ctr;
     da.acc = acc;
-    if (ctx->precision == DMANN_COMP_F32) da.chdr = (CompHdr *)ctx->chdr.p;
+    if (ctx->precision == DMANN_COMP_F32) da.chdr = headers_for(ctx, N);
     CK(cudaEventRecord(ctx->evd0, s));
     if (ctx->precision == DMANN_PLAIN_F64) CK(launch_disc_plain(da, ctx->num_sms, tu.blocks_per_sm, s, ctx->evdm));
     else CK(launch_disc_comp(da, ctx->num_sms, tu.blocks_per_sm, tu.block_threads, s, ctx->evdm));
@@ -782,7 +806,7 @@ dmann_status issue_observer(dmann_ctx *ctx, const float *const dev[6], int n, in
         da.queue = (const int *)ctx->queue.p;
         da.ctr = pa.ctr;
         da.acc = acc;
-        if (precision == DMANN_COMP_F32) da.chdr = (CompHdr *)ctx->chdr.p;
+        if (precision == DMANN_COMP_F32) da.chdr = headers_for(ctx, (size_t)n);
         if (precision == DMANN_PLAIN_F64) CK(launch_disc_plain(da, ctx->num_sms, tu.blocks_per_sm, s, nullptr));
         else CK(launch_disc_comp(da, ctx->num_sms, tu.blocks_per_sm, tu.block_threads, s, nullptr));
     }
@@ -828,8 +852,7 @@ dmann_status dmann_render_batch(dmann_ctx *ctx, const float *x, const float *y, 
         (st = ensure(ctx, ctx->ctr, 8 * C_COUNT)) || (st = ensure(ctx, ctx->fsum, 8)) ||
         (st = ensure(ctx, ctx->acc, 8 * Pmax)) || (st = ensure(ctx, ctx->map, 8 * Pmax)))
         return st;
-    if (precision == DMANN_COMP_F32 && (st = ensure(ctx, ctx->chdr, comp_hdr_bytes() * n1)))
-        return st;
+    if (precision == DMANN_COMP_F32) reserve_headers(ctx, n1);   // before any capture
     std::vector<RingTables> rts(n_obs);
     for (int k = 0; k < n_obs; k++)
         if ((st = ring_tables(ctx, nside[k], rts[k])) != DMANN_OK) return st;
@@ -941,9 +964,10 @@ dmann_status dmann_adjoint(dmann_ctx *ctx, const float *x, const float *y, const
         (st = ensure(ctx, ctx->hist, 4 * (size_t)kKeys)) || (st = ensure(ctx, ctx->ctr, 8 * C_COUNT)) ||
         (st = ensure(ctx, ctx->fsum, 8)) || (st = ensure(ctx, ctx->oacc, 8 * 12)))
         return st;
-    if (precision == DMANN_COMP_F32 && ((st = ensure(ctx, ctx->acc, 4 * P)) ||
-                                        (st = ensure(ctx, ctx->chdr, comp_hdr_bytes() * n1))))
-        return st;
+    if (precision == DMANN_COMP_F32) {
+        if ((st = ensure(ctx, ctx->acc, 4 * P)) != DMANN_OK) return st;
+        reserve_headers(ctx, n1);
+    }
     const float *src[6] = {x, y, z, m, rho, h};
     const float *dev[6];
     for (int k = 0; k < 6; k++) {
@@ -1005,7 +1029,7 @@ dmann_status dmann_adjoint(dmann_ctx *ctx, const float *x, const float *y, const
     da.queue = (const int *)ctx->queue.p;
     da.ctr = pa.ctr;
     da.acc = pa.acc;
-    if (precision == DMANN_COMP_F32) da.chdr = (CompHdr *)ctx->chdr.p;
+    if (precision == DMANN_COMP_F32) da.chdr = headers_for(ctx, n1);
     CK(cudaEventRecord(ctx->evd0, s));
     CK(launch_adjoint(da, pa.p, pa.out.cls, dgmap, (float *)ctx->acc.p, dgrad, (double *)ctx->oacc.p,
                       precision, ctx->num_sms, s));
