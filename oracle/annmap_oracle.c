@@ -470,11 +470,17 @@ static double pixel_weight(const orc_hpx *hb, int32_t pix, const double v[3], do
 
 double orc_particle_loss(const orc_params *p, double mass, double dens, double hsmooth,
                          double x, double y, double z, const double *G, uint64_t *sig) {
+    return orc_particle_loss_v(p, mass, dens, hsmooth, x, y, z, 0.0, G, sig);
+}
+
+double orc_particle_loss_v(const orc_params *p, double mass, double dens, double hsmooth,
+                           double x, double y, double z, double sigmav, const double *G,
+                           uint64_t *sig) {
     orc_hpx hb;
     orc_hpx_init(&hb, p->nside);
     geom_t g;
     memset(&g, 0, sizeof g);
-    particle_geom_d(p, &hb, mass, dens, hsmooth, x, y, z, &g);
+    particle_geom_dv(p, &hb, mass, dens, hsmooth, x, y, z, sigmav, &g);
     uint64_t hsig = 1469598103934665603ull; /* FNV-1a over the branch and pixels */
 #define SIG(v) do { hsig ^= (uint64_t)(v); hsig *= 1099511628211ull; } while (0)
     double L = 0.0;
@@ -519,11 +525,28 @@ void orc_particle_losses(const orc_params *p, const double *mass, const double *
                                  sig ? sig + i : NULL);
 }
 
+void orc_particle_losses_v(const orc_params *p, const double *mass, const double *dens,
+                           const double *hsmooth, const double *x, const double *y,
+                           const double *z, const double *sigmav, int64_t n, const double *G,
+                           double *L, uint64_t *sig) {
+    for (int64_t i = 0; i < n; i++)
+        L[i] = orc_particle_loss_v(p, mass[i], dens[i], hsmooth[i], x[i], y[i], z[i],
+                                   sigmav ? sigmav[i] : 0.0, G, sig ? sig + i : NULL);
+}
+
 int orc_adjoint(const orc_params *p, const float *mass, const float *dens,
                 const float *hsmooth, const float *x, const float *y, const float *z,
                 int64_t n, const double *G, double *grad, double oacc[12]) {
-    /* laws whose flux is rho m (or m) times a constant over d^2 */
-    if (p->flux_model != 0 && p->flux_model != 4) return -2;
+    return orc_adjoint_v(p, mass, dens, hsmooth, x, y, z, NULL, n, G, grad, oacc);
+}
+
+int orc_adjoint_v(const orc_params *p, const float *mass, const float *dens,
+                  const float *hsmooth, const float *x, const float *y, const float *z,
+                  const float *sigmav, int64_t n, const double *G, double *grad,
+                  double oacc[12]) {
+    /* laws whose flux is rho m (or m) times a factor of sigma v alone over
+       d^2: nosom, somv, somv2, pwave, decay */
+    if (p->flux_model < 0 || p->flux_model > 4) return -2;
     orc_hpx hb;
     orc_hpx_init(&hb, p->nside);
     int32_t *list = (int32_t *)malloc(sizeof(int32_t) * (size_t)p->npix);
@@ -533,7 +556,9 @@ int orc_adjoint(const orc_params *p, const float *mass, const float *dens,
     for (int64_t i = 0; i < n; i++) {
         for (int k = 0; k < 6; k++) grad[k * n + i] = 0.0;
         geom_t g;
-        particle_geom(p, &hb, mass[i], dens[i], hsmooth[i], x[i], y[i], z[i], &g);
+        const double sv = sigmav ? (double)sigmav[i] : 0.0;
+        particle_geom_dv(p, &hb, (double)mass[i], (double)dens[i], (double)hsmooth[i],
+                         (double)x[i], (double)y[i], (double)z[i], sv, &g);
         if (!g.kept || !(g.d > 0.0) || !isfinite(g.flux) || !isfinite(g.ar)) continue;
         double Gb, KT = 0.0, KV[3] = {0.0, 0.0, 0.0};
         int64_t npd = disc_pixels(p, &hb, &g, list);
@@ -570,10 +595,11 @@ int orc_adjoint(const orc_params *p, const float *mass, const float *dens,
                        (double)z[i] - p->obs_pos[2]};
         double d = g.d;
         double uh[3] = {u[0] / d, u[1] / d, u[2] / d};
-        /* F = fd rho m (nosom), or fd m with the decay law's own unit factor
+        /* F = fd rho m with fd the law's flux per unit rho m (its sigma v
+           factor included), or fd m under the decay law
            (src/flux/flux_decay.cpp:9-16): then dL/drho = 0 */
         int decay = p->flux_model == 4;
-        double fd = (decay ? p->decay_unit_factor : p->unit_factor) / (4.0 * PI * d * d);
+        double fd = orc_flux(p, 1.0, 1.0, sv, (double)x[i], (double)y[i], (double)z[i], d);
         double rho_f = decay ? 1.0 : (double)dens[i];
         double F = fd * rho_f * (double)mass[i];
         double w[3] = {-KV[0], -KV[1], KV[2]}; /* D K V, D = diag(-1,-1,1) */

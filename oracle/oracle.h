@@ -150,6 +150,18 @@ void orc_particle_geom(const orc_params *p, float mass, float dens,
 double orc_particle_loss(const orc_params *p, double mass, double dens, double hsmooth,
                          double x, double y, double z, const double *G, uint64_t *sig);
 
+/* orc_particle_loss with a velocity dispersion (the somv, somv2 and pwave
+ * laws). */
+double orc_particle_loss_v(const orc_params *p, double mass, double dens, double hsmooth,
+                           double x, double y, double z, double sigmav, const double *G,
+                           uint64_t *sig);
+
+/* orc_particle_loss_v over n particles (sigmav may be NULL). */
+void orc_particle_losses_v(const orc_params *p, const double *mass, const double *dens,
+                           const double *hsmooth, const double *x, const double *y,
+                           const double *z, const double *sigmav, int64_t n, const double *G,
+                           double *L, uint64_t *sig);
+
 /* orc_particle_loss over n particles (double SoA inputs). */
 void orc_particle_losses(const orc_params *p, const double *mass, const double *dens,
                          const double *hsmooth, const double *x, const double *y,
@@ -157,10 +169,18 @@ void orc_particle_losses(const orc_params *p, const double *mass, const double *
                          uint64_t *sig);
 
 /* grad = [6][n] (x, y, z, m, rho, h); oacc[0..2] = sum_i dL/du_i,
- * oacc[3..11] = dL/drot (row-major).  Returns 0 on success. */
+ * oacc[3..11] = dL/drot (row-major).  Returns 0 on success, -2 for a flux
+ * law whose flux is not rho m (or m) times a factor of sigma v over d^2. */
 int orc_adjoint(const orc_params *p, const float *mass, const float *dens,
                 const float *hsmooth, const float *x, const float *y, const float *z,
                 int64_t n, const double *G, double *grad, double oacc[12]);
+
+/* The same with the velocity dispersions of the somv, somv2 and pwave laws
+ * (sigmav may be NULL: zero); sigma v is not differentiated. */
+int orc_adjoint_v(const orc_params *p, const float *mass, const float *dens,
+                  const float *hsmooth, const float *x, const float *y, const float *z,
+                  const float *sigmav, int64_t n, const double *G, double *grad,
+                  double oacc[12]);
 
 #ifdef __cplusplus
 }

@@ -106,6 +106,11 @@ def lib():
             L.orc_adjoint.argtypes = [P(OrcParams), f32, f32, f32, f32, f32, f32, C.c_int64,
                                       P(C.c_double), P(C.c_double), P(C.c_double)]
             L.orc_adjoint.restype = C.c_int
+            L.orc_particle_losses_v.argtypes = [P(OrcParams), d64, d64, d64, d64, d64, d64, d64,
+                                                C.c_int64, d64, d64, P(C.c_uint64)]
+            L.orc_adjoint_v.argtypes = [P(OrcParams), f32, f32, f32, f32, f32, f32, f32, C.c_int64,
+                                        P(C.c_double), P(C.c_double), P(C.c_double)]
+            L.orc_adjoint_v.restype = C.c_int
             _LIB = L
     return _LIB
 
@@ -239,7 +244,11 @@ def adjoint(p: OrcParams, parts: dict, G) -> tuple:
     G = np.ascontiguousarray(G, dtype=np.float64)
     grad = np.zeros((6, n), dtype=np.float64)
     oacc = np.zeros(12, dtype=np.float64)
-    rc = lib().orc_adjoint(C.byref(p), *ptrs, n, _dptr(G), _dptr(grad), _dptr(oacc))
+    if parts.get("sigmav") is not None:     # the somv, somv2 and pwave laws
+        sv, svp = _f32(parts["sigmav"])
+        rc = lib().orc_adjoint_v(C.byref(p), *ptrs, svp, n, _dptr(G), _dptr(grad), _dptr(oacc))
+    else:
+        rc = lib().orc_adjoint(C.byref(p), *ptrs, n, _dptr(G), _dptr(grad), _dptr(oacc))
     if rc != 0:
         raise RuntimeError("oracle adjoint failed")
     return grad, oacc
@@ -261,8 +270,14 @@ def particle_losses(p: OrcParams, parts: dict, G) -> tuple:
     G = np.ascontiguousarray(G, dtype=np.float64)
     L = np.zeros(n)
     sig = np.zeros(n, dtype=np.uint64)
-    lib().orc_particle_losses(C.byref(p), *[_dptr(a) for a in arrs], n, _dptr(G), _dptr(L),
-                              sig.ctypes.data_as(C.POINTER(C.c_uint64)))
+    sigp = sig.ctypes.data_as(C.POINTER(C.c_uint64))
+    if parts.get("sigmav") is not None:     # the somv, somv2 and pwave laws
+        sv = np.ascontiguousarray(parts["sigmav"], dtype=np.float64)
+        lib().orc_particle_losses_v(C.byref(p), *[_dptr(a) for a in arrs], _dptr(sv), n, _dptr(G),
+                                    _dptr(L), sigp)
+    else:
+        lib().orc_particle_losses(C.byref(p), *[_dptr(a) for a in arrs], n, _dptr(G), _dptr(L),
+                                  sigp)
     return L, sig
 
 

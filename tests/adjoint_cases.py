@@ -54,6 +54,8 @@ def fd_check(p, parts, G, grad, rel_eps=1e-5):
     sides are left out.  Returns {field: (norm-wise relative error, number
     of particles compared)}."""
     d64 = {k: np.asarray(parts[k], dtype=np.float64) for k in FIELDS}
+    if parts.get("sigmav") is not None:   # carried along, not differentiated
+        d64["sigmav"] = np.asarray(parts["sigmav"], dtype=np.float64)
     out = {}
     for kk, k in enumerate(FIELDS):
         eps = rel_eps * (d64["h"] if k in ("x", "y", "z") else np.abs(d64[k]))

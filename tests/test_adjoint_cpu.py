@@ -121,10 +121,41 @@ def test_oracle_adjoint_decay_law(decay_case):
     assert np.sum(m * grad[3]) == pytest.approx(L, rel=1e-10)
 
 
-def test_oracle_adjoint_rejects_other_laws():
+def test_oracle_adjoint_rejects_position_dependent_laws():
+    """adiabatic and ann_core_nosom boost the flux by a function of the
+    particle's position, which the adjoint does not differentiate."""
     P, parts, p0 = make_case(200, 32, seed=3)
-    for law in (1, 2, 3, 5, 6):
+    for law in (5, 6):
         p = O.make_params(nside=32, obs_pos=P.obs_pos, centerpos=P.centerpos,
                           align_vec=P.align_vec, particle_masses=(P.particle_mass,), flux_model=law)
         with pytest.raises(RuntimeError):
             O.adjoint(p, parts, np.ones(12 * 32 * 32))
+
+
+@pytest.mark.parametrize("law", [1, 2, 3], ids=["somv", "somv2", "pwave"])
+def test_oracle_adjoint_sigma_v_laws(law):
+    """somv, somv2, pwave: flux = rho m f(sigma v) / d^2 with sigma v held
+    fixed (it is not differentiated); velocity dispersions straddle the
+    somv / somv2 saturation speeds."""
+    P, parts, p0 = make_case(2000, 128, seed=41 + law, single_frac=0.2, skipped=20)
+    p = O.make_params(nside=128, obs_pos=P.obs_pos, centerpos=P.centerpos, align_vec=P.align_vec,
+                      particle_masses=(P.particle_mass,), flux_model=law)
+    rng = np.random.default_rng(law)
+    kms = 1e5 / p.velocity_to_cgs                      # 1 km/s in code units
+    parts = dict(parts, sigmav=(rng.uniform(0.2, 12.0, len(P)) * kms).astype(np.float32))
+    mp, _, _ = O.render(p, parts)
+    target, _, _ = O.render(p, dict(__import__("adjoint_cases").jittered(P), sigmav=parts["sigmav"]))
+    _, G = loss_grad(mp, target)
+    grad, oacc = O.adjoint(p, parts, G)
+    res = fd_check(p, parts, G, grad)
+    for k in FIELDS:
+        err, n_ok = res[k]
+        assert n_ok > 1600, (k, n_ok)
+        assert err < 1e-6, (k, err)
+    L = float(np.dot(G, mp))
+    m, rho = (parts[k].astype(np.float64) for k in ("m", "rho"))
+    assert np.sum(m * grad[3]) == pytest.approx(L, rel=1e-10)
+    assert np.sum(rho * grad[4]) == pytest.approx(L, rel=1e-10)
+    # without sigma v these laws' fluxes differ, and so does the gradient
+    g0, _ = O.adjoint(p, {k: v for k, v in parts.items() if k != "sigmav"}, G)
+    assert np.linalg.norm(g0[3] - grad[3]) > 0.1 * np.linalg.norm(grad[3]) > 0
