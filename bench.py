@@ -34,7 +34,7 @@ import numpy as np  # noqa: E402
 METRIC = "particles/s at Nside 2048: comp-FP32 vs plain GPU form; px err vs FP64"
 UNIT = "particles/s"
 WORKLOAD = "nfw16m_sub100_ns2048"
-KERNELS_PER_STEP = 6  # prep, key scan, queue scatter, disc (block), disc (warp), finalize
+KERNELS_PER_STEP = 7  # prep, key scan, queue scatter, disc headers, disc (block), disc (warp), finalize
 
 
 def parse():
