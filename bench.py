@@ -1,6 +1,6 @@
 """Benchmark of the annihilation sky-map projection on GB300.
 
-Headline metric (the benchmark spec): particles/s at Nside 2048 for the
+Headline metric: particles/s at Nside 2048 for the
 compensated-FP32 form, with the plain FP64-accumulate GPU form and the
 per-pixel error against FP64 reported beside it.  Workload: the 16,777,216-
 particle NFW host + 100 subhalos set (seeded synthetic stand-in for the

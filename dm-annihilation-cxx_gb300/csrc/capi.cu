@@ -71,6 +71,7 @@ struct dmann_ctx {
     RingTables rt;
     int precision = DMANN_COMP_F32;
     bool in_map = false;
+    int64_t launches = 0;   // kernels launched for the current / last map
     std::string err;
 };
 
@@ -248,6 +249,7 @@ dmann_status collect_stats(dmann_ctx *ctx) {
     ctx->stats.n_disc_block = ctx->h_ctr[C_DISC_BLOCK];
     ctx->stats.deposits = ctx->h_ctr[C_DEPOSITS];
     ctx->stats.total_flux = *ctx->h_fsum;
+    ctx->stats.launches = ctx->launches;
     ctx->stats_pending = false;
     return DMANN_OK;
 }
@@ -554,7 +556,7 @@ dmann_status check_particles(dmann_ctx *ctx, const float *x, const float *y, con
 }
 
 Frame make_frame(const dmann_ctx *ctx, double *scale) {
-    Frame f;
+    Frame f{};
     for (int i = 0; i < 3; i++)
         for (int j = 0; j < 3; j++) f.rot[i][j] = ctx->rot[3 * i + j];
     for (int i = 0; i < 3; i++) f.opos[i] = ctx->opos[i];
@@ -582,6 +584,12 @@ Accum make_accum(dmann_ctx *ctx) {
 
 }  // namespace
 
+// Every context call that uses the accumulation planes, the queue or the
+// counters refuses to run while a streamed map is open: it would zero or
+// reuse the buffers the open map is accumulating into.
+const char *const map_open_msg =
+    "a streamed map is in progress: dmann_map_end or dmann_map_abort it first";
+
 dmann_status dmann_map_begin(dmann_ctx *ctx, int nside, int precision) {
     if (!ctx) return DMANN_ERR_INVALID;
     if (nside < 1 || nside > 8192) return fail(ctx, DMANN_ERR_INVALID, "nside must be in [1, 8192]");
@@ -589,6 +597,7 @@ dmann_status dmann_map_begin(dmann_ctx *ctx, int nside, int precision) {
         return fail(ctx, DMANN_ERR_INVALID, "unknown precision form");
     if (!ctx->have_frame) return fail(ctx, DMANN_ERR_STATE, "observer frame not set");
     if (!ctx->have_units) return fail(ctx, DMANN_ERR_STATE, "units not set");
+    if (ctx->in_map) return fail(ctx, DMANN_ERR_STATE, map_open_msg);
     CK(cudaSetDevice(ctx->device));
     dmann_status st = collect_stats(ctx);
     if (st != DMANN_OK) return st;
@@ -605,6 +614,7 @@ dmann_status dmann_map_begin(dmann_ctx *ctx, int nside, int precision) {
     CK(cudaMemsetAsync(ctx->ctr.p, 0, 8 * C_COUNT, s));
     CK(cudaMemsetAsync(ctx->fsum.p, 0, 8, s));
     ctx->stats = dmann_stats{};
+    ctx->launches = 0;
     ctx->disc_timed = false;
     ctx->in_map = true;
     return DMANN_OK;
@@ -664,6 +674,7 @@ dmann_status dmann_map_add_v(dmann_ctx *ctx, const float *x, const float *y, con
         if ((st = ensure(ctx, ctx->corr, 8 * N)) != DMANN_OK) return st;
         CK(launch_halo_core(ctx->halo, pa.p, (double *)ctx->corr.p, s));
         pa.core_corr = (const double *)ctx->corr.p;
+        ctx->launches++;
     }
     pa.f = f;
     pa.g = ctx->g;
@@ -697,6 +708,8 @@ dmann_status dmann_map_add_v(dmann_ctx *ctx, const float *x, const float *y, con
     if (ctx->precision == DMANN_PLAIN_F64) CK(launch_disc_plain(da, ctx->num_sms, tu.blocks_per_sm, s, ctx->evdm));
     else CK(launch_disc_comp(da, ctx->num_sms, tu.blocks_per_sm, tu.block_threads, s, ctx->evdm));
     CK(cudaEventRecord(ctx->evd1, s));
+    // prep, scan, scatter, the disc kernels (block, warp; headers when held)
+    ctx->launches += 5 + (da.chdr ? 1 : 0);
     ctx->disc_timed = true;
     return DMANN_OK;
 }
@@ -720,6 +733,7 @@ dmann_status dmann_map_end(dmann_ctx *ctx, double *map_out, int accumulate) {
     (void)make_frame(ctx, &scale);
     CK(launch_finalize(make_accum(ctx), ctx->precision, ctx->g.npix, ctx->g.dOmega, scale, dmap,
                        accumulate, s));
+    ctx->launches++;
     CK(cudaEventRecord(ctx->ev1, s));
     CK(cudaMemcpyAsync(ctx->h_ctr, ctx->ctr.p, 8 * C_COUNT, cudaMemcpyDeviceToHost, s));
     CK(cudaMemcpyAsync(ctx->h_fsum, ctx->fsum.p, 8, cudaMemcpyDeviceToHost, s));
@@ -729,6 +743,12 @@ dmann_status dmann_map_end(dmann_ctx *ctx, double *map_out, int accumulate) {
         CK(cudaMemcpyAsync(map_out, dmap, 8 * P, cudaMemcpyDeviceToHost, s));
         CK(cudaStreamSynchronize(s));
     }
+    return DMANN_OK;
+}
+
+dmann_status dmann_map_abort(dmann_ctx *ctx) {
+    if (!ctx) return DMANN_ERR_INVALID;
+    ctx->in_map = false;
     return DMANN_OK;
 }
 
@@ -828,6 +848,7 @@ dmann_status dmann_render_batch(dmann_ctx *ctx, const float *x, const float *y, 
     if (precision != DMANN_PLAIN_F64 && precision != DMANN_COMP_F32)
         return fail(ctx, DMANN_ERR_INVALID, "unknown precision form");
     if (!ctx->have_units) return fail(ctx, DMANN_ERR_STATE, "units not set");
+    if (ctx->in_map) return fail(ctx, DMANN_ERR_STATE, map_open_msg);
     if (law_needs_sigmav(ctx->flux_model))
         return fail(ctx, DMANN_ERR_INVALID, "the batch takes no velocity dispersion: render this flux law per observer");
     dmann_status st = check_particles(ctx, x, y, z, m, rho, h, n);
@@ -946,6 +967,7 @@ dmann_status dmann_adjoint(dmann_ctx *ctx, const float *x, const float *y, const
     if (nside < 1 || nside > 8192) return fail(ctx, DMANN_ERR_INVALID, "nside must be in [1, 8192]");
     if (!ctx->have_frame) return fail(ctx, DMANN_ERR_STATE, "observer frame not set");
     if (!ctx->have_units) return fail(ctx, DMANN_ERR_STATE, "units not set");
+    if (ctx->in_map) return fail(ctx, DMANN_ERR_STATE, map_open_msg);
     if (ctx->flux_model != DMANN_FLUX_ANN_NOSOM && ctx->flux_model != DMANN_FLUX_DECAY)
         return fail(ctx, DMANN_ERR_INVALID, "the adjoint supports the nosom and decay flux laws only");
     dmann_status st = check_particles(ctx, x, y, z, m, rho, h, n);

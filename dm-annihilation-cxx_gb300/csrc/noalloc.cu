@@ -182,7 +182,7 @@ extern "C" dmann_status dmann_render_noalloc(const float *x, const float *y, con
     g.dOmega = 4 * 3.14159265358979323846 / (double)npix;  // src/datatypes.h:251
     g.theta0 = std::acos(1.0 - g.dOmega / (2.0 * 3.141592));  // src/genmap.cpp:38
 
-    Frame f;
+    Frame f{};   // every field defined, including those the nosom law never reads
     for (int i = 0; i < 3; i++) {
         for (int j = 0; j < 3; j++) f.rot[i][j] = rot[3 * i + j];
         f.opos[i] = opos[i];

@@ -34,7 +34,7 @@ class Stats(C.Structure):
                 ("n_disc", C.c_int64), ("n_disc_block", C.c_int64), ("deposits", C.c_int64),
                 ("kernel_ms", C.c_double), ("disc_ms", C.c_double),
                 ("disc_block_ms", C.c_double), ("disc_warp_ms", C.c_double),
-                ("total_flux", C.c_double)]
+                ("total_flux", C.c_double), ("launches", C.c_int64)]
 
 
 class Tuning(C.Structure):
@@ -68,6 +68,7 @@ SIGNATURES = {
     "dmann_map_begin": (C.c_int, [_P, C.c_int, C.c_int]),
     "dmann_map_add": (C.c_int, [_P, _P, _P, _P, _P, _P, _P, C.c_int64]),
     "dmann_map_end": (C.c_int, [_P, _P, C.c_int]),
+    "dmann_map_abort": (C.c_int, [_P]),
     "dmann_map_add_v": (C.c_int, [_P, _P, _P, _P, _P, _P, _P, _P, C.c_int64]),
     "dmann_render_v": (C.c_int, [_P, _P, _P, _P, _P, _P, _P, _P, C.c_int64, C.c_int, C.c_int, _P, C.c_int]),
     "dmann_set_flux_params": (C.c_int, [_P, C.c_double, _D3]),

@@ -187,10 +187,19 @@ class Renderer:
             self._keep = []
         return out
 
+    def abort(self):
+        """Closes an open streamed map without output (dmann_map_abort)."""
+        self._check(self.L.dmann_map_abort(self.ctx))
+        self._keep = []
+
     def render(self, parts: dict, nside: int, precision: int = COMP_F32, out=None,
                accumulate: bool = False):
         self.begin(nside, precision)
-        self.add(parts)
+        try:
+            self.add(parts)
+        except BaseException:
+            self.abort()
+            raise
         return self.end(out, accumulate)
 
     def render_batch(self, parts: dict, frames, nsides, precision: int = COMP_F32, outs=None):
@@ -282,8 +291,12 @@ class MapGenerator:
                 from .halocore import read_halo_table
                 r.set_halo_cores(*read_halo_table(self.halo_file))
             r.begin(self.par_.map.Nside, self.precision)
-            while self.reader_.hasNext():
-                r.add(self.reader_.next_chunk())
+            try:
+                while self.reader_.hasNext():
+                    r.add(self.reader_.next_chunk())
+            except BaseException:
+                r.abort()
+                raise
             self.map_ = r.end()
             st = r.stats()
             self.total_flux = st["total_flux"]  # the reference's "Total Conts"

@@ -107,13 +107,16 @@ class DataReader:
     def hasNext(self) -> bool:
         return self._open and self._cursor < self._n
 
-    def next_chunk(self) -> dict:
-        """The next chunk as float32 SoA arrays x, y, z, m, rho, h."""
+    def next_chunk(self, velocities: bool = False) -> dict:
+        """The next chunk as float32 SoA arrays x, y, z, m, rho, h and sigmav;
+        with ``velocities`` also the velocity components vx, vy, vz."""
         i0 = self._cursor
         i1 = min(self._n, i0 + self.memBuffer)
         rec = np.asarray(self._mm[i0:i1])
         if self._tipsy is not None:
             out = {"x": rec["posx"], "y": rec["posy"], "z": rec["posz"], "m": rec["mass"]}
+            if velocities:
+                out.update({"vx": rec["velx"], "vy": rec["vely"], "vz": rec["velz"]})
             out = {k: np.ascontiguousarray(v, dtype=np.float32) for k, v in out.items()}
             if self._side is None:
                 z = np.zeros(i1 - i0, np.float32)
@@ -130,10 +133,13 @@ class DataReader:
             rho = rho.copy()
             rho[np.asarray(self._mask[i0:i1]) == 0] = -1.0
         self._cursor = i1
-        return {"x": np.ascontiguousarray(rec["posx"]), "y": np.ascontiguousarray(rec["posy"]),
-                "z": np.ascontiguousarray(rec["posz"]), "m": np.ascontiguousarray(rec["mass"]),
-                "rho": rho, "h": np.ascontiguousarray(rec["hsmooth"]),
-                "sigmav": np.ascontiguousarray(rec["sigmav"])}
+        out = {"x": np.ascontiguousarray(rec["posx"]), "y": np.ascontiguousarray(rec["posy"]),
+               "z": np.ascontiguousarray(rec["posz"]), "m": np.ascontiguousarray(rec["mass"]),
+               "rho": rho, "h": np.ascontiguousarray(rec["hsmooth"]),
+               "sigmav": np.ascontiguousarray(rec["sigmav"])}
+        if velocities:
+            out.update({k: np.ascontiguousarray(rec["vel" + k[1]]) for k in ("vx", "vy", "vz")})
+        return out
 
     def close(self):
         self._mm = None

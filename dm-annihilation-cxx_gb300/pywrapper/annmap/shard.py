@@ -2,11 +2,9 @@
 
 Particles are independent and the map is a sum over them, so N ranks can
 each render a contiguous 1/N of the particles into a full partial map and
-one sum reduction of the FP64 maps gives the whole map (SURVEY §8(e)'s first
-partitioning).  Each rank's shard is [n*r/N, n*(r+1)/N).  Every machine in
-this fleet has one GPU, so the benchmark runs replicas instead; this module
-is the data path a multi-GPU node would use (NCCL on CUDA tensors), and its
-arithmetic is tested with gloo ranks on the CPU.
+one sum reduction of the FP64 maps gives the whole map.  Each rank's shard
+is [n*r/N, n*(r+1)/N).  This is the data path of a node with several GPUs
+(NCCL on CUDA tensors); its arithmetic is tested with gloo ranks on the CPU.
 """
 from __future__ import annotations
 

@@ -19,7 +19,11 @@ Generator (all draws from ``numpy.random.Generator(PCG64(seed))``):
     h = (32 m / (4 pi/3 rho))^(1/3) (the 32-neighbour SPH convention);
   * optional ``near_observer`` particles uniform within ``near_radius`` of
     the observer, with the host density there (the large-disc case);
-  * the particle order is shuffled, so any prefix is an i.i.d. sample.
+  * the particle order is shuffled, so any prefix is an i.i.d. sample;
+  * ``n_total`` draws the n particles as an i.i.d. sample of an n_total-
+    particle set: densities (hence smoothing lengths) are normalised to the
+    larger set's particle counts, so the sample has its per-particle disc
+    statistics without generating it whole.
 """
 from __future__ import annotations
 
@@ -107,7 +111,7 @@ def default_observer():
 
 def nfw_halo(n: int, *, seed: int, n_sub: int = 0, sub_frac: float = 0.1,
              particle_mass: float = 4.1e3, near_observer: int = 0, near_radius: float = 0.5,
-             obs_pos=None, shuffle: bool = True) -> Particles:
+             obs_pos=None, shuffle: bool = True, n_total: int | None = None) -> Particles:
     """Builds an ``n``-particle set (see the module docstring)."""
     rng = np.random.Generator(np.random.PCG64(seed))
     obs = np.array(obs_pos if obs_pos is not None else default_observer(), dtype=np.float64)
@@ -127,7 +131,9 @@ def nfw_halo(n: int, *, seed: int, n_sub: int = 0, sub_frac: float = 0.1,
             order = np.argsort(-(share - counts))
             counts[order[:rem]] += 1
     n_host = n_halo - int(counts.sum())
-    m_host = n_host * m
+    # the set the particles are a sample of (itself unless n_total is given)
+    grow = 1.0 if n_total is None else float(n_total) / float(n)
+    m_host = n_host * m * grow
 
     pos_l, rho_l, h_l = [], [], []
     chunk = 1 << 22
@@ -144,7 +150,7 @@ def nfw_halo(n: int, *, seed: int, n_sub: int = 0, sub_frac: float = 0.1,
             if k == 0:
                 continue
             r200s = R200_HOST * (msub[j] / m_host) ** (1.0 / 3.0)
-            p, r, h = _nfw_sample(rng, k, r200s / CONC, CONC, k * m, centres[j], m)
+            p, r, h = _nfw_sample(rng, k, r200s / CONC, CONC, k * m * grow, centres[j], m)
             pos_l.append(p); rho_l.append(r); h_l.append(h)
     if n_near > 0:
         d = near_radius * np.cbrt(rng.uniform(0.0, 1.0, n_near))

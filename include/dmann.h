@@ -44,7 +44,7 @@
 extern "C" {
 #endif
 
-#define DMANN_ABI_VERSION 1
+#define DMANN_ABI_VERSION 2
 
 typedef struct dmann_ctx dmann_ctx;
 
@@ -104,6 +104,7 @@ typedef struct {
     double disc_block_ms;  /* of which the block-per-particle kernel */
     double disc_warp_ms;   /* of which the warp-per-particle kernel */
     double total_flux;     /* sum of kept flux (before the dOmega division) */
+    int64_t launches;      /* kernels launched for the last map (all chunks) */
 } dmann_stats;
 
 /* Tunables (set by the annmap autotuner; zero fields keep the current
@@ -204,12 +205,19 @@ dmann_status dmann_render_v(dmann_ctx *ctx, const float *x, const float *y,
  * chunk of particles into them (inputs host or device), end divides by
  * dOmega into map_out (host or device; accumulate != 0 adds to it).  The
  * FP64 plane carries the sum across chunks, so a streamed map equals a
- * single-call one to the rounding of the FP64 additions. */
+ * single-call one to the rounding of the FP64 additions.
+ *
+ * While a map is open (after begin, until end or abort) the context's
+ * buffers belong to it: dmann_map_begin, dmann_render(_v),
+ * dmann_render_batch and dmann_adjoint on the same context fail with
+ * DMANN_ERR_STATE.  dmann_map_abort closes an open map without output (for
+ * instance after a failed add); the next begin starts from zero. */
 dmann_status dmann_map_begin(dmann_ctx *ctx, int nside, int precision);
 dmann_status dmann_map_add(dmann_ctx *ctx, const float *x, const float *y,
                            const float *z, const float *m, const float *rho,
                            const float *h, int64_t n);
 dmann_status dmann_map_end(dmann_ctx *ctx, double *map_out, int accumulate);
+dmann_status dmann_map_abort(dmann_ctx *ctx);
 /* dmann_map_add with the velocity dispersion (as dmann_render_v). */
 dmann_status dmann_map_add_v(dmann_ctx *ctx, const float *x, const float *y,
                              const float *z, const float *m, const float *rho,

@@ -1,7 +1,7 @@
 /*
  * annmap_oracle.c -- FP64 CPU restatement of the reference's CPU map path.
  *
- * TEST INFRASTRUCTURE ONLY (see oracle.h): used by the tests as the checker,
+ * TEST INFRASTRUCTURE ONLY (see oracle.h): used by the tests as the reference answer,
  * by the smoke check, and as the timed CPU baseline of the benchmark.  The
  * product never links or calls it.
  *

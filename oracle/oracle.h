@@ -4,7 +4,7 @@
  * TEST INFRASTRUCTURE ONLY.  Nothing in the product (the CUDA library, the
  * C++ host API, the Python package) links, loads or calls this code.  Only
  * the test suite, the smoke check and the CPU-baseline leg of the benchmark
- * use it, and only as the checker / the timed CPU reference.
+ * use it, and only as the reference answer / the timed CPU baseline.
  *
  * What it restates (paths relative to the reference project):
  *   - src/genmap.cpp:22-175            MapGenerator::start, the CPU map loop

@@ -1,7 +1,7 @@
 """ctypes loader for the FP64 CPU oracle (oracle/liboracle.so).
 
 TEST INFRASTRUCTURE ONLY.  The test suite, the smoke check and the
-CPU-baseline leg of ``bench.py`` import this module as the checker; the
+CPU-baseline leg of ``bench.py`` import this module as the reference answer; the
 product (the CUDA library and the ``annmap`` package) never does.
 
 The oracle restates the reference's CPU map path; see oracle.h for the file

@@ -32,6 +32,8 @@ REF_BIN = os.path.join(REPO, "oracle", "_ref", "annmap_ref")
 
 
 def build_ref():
+    # the reference sources: DMANN_REF_SRC, else a `reference` checkout beside
+    # this repository (the Makefile's default)
     subprocess.run(["make", "-s", "-C", os.path.join(REPO, "oracle", "ref_shim")], check=True)
 
 

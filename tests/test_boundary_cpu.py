@@ -40,7 +40,7 @@ def test_library_exports_every_declared_symbol():
 
 
 def test_abi_version():
-    assert _lib.load().dmann_abi_version() == 1
+    assert _lib.load().dmann_abi_version() == 2
 
 
 def test_no_gpu_fails_loudly():

@@ -6,8 +6,12 @@ cannot afford cudaMalloc's implicit synchronisation.  For them the library
 offers one entry point that works entirely in a fixed scratch array compiled
 into it.  These tests call it through the C ABI on device buffers and check its
 map against the ordinary compensated render (dmann_render through a context),
-on two calls in a row, with the tolerance the other compensated-form tests use
-for run-to-run differences (the atomics' order: ~1e-11 relative).
+on two calls in a row.  The two are independent renders, so they differ by the
+compensated form's run-to-run spread: the order in which warps claim rings
+can move a particle's normalisation by ~1e-13 relative, which can flip the
+one FP32 rounding of a deposit near a rounding boundary (at most 2^-24 of
+that deposit), and the FP64 reductions add in a different order.  RTOL is the
+bound the other run-to-run comparisons of the compensated form use.
 
 This file is named to be collected last, so a run that stops at the first
 failure has run everything else first; it also passes on its own.
@@ -22,7 +26,7 @@ from annmap import _lib, synth
 
 pytestmark = pytest.mark.gpu
 
-RTOL = 1e-10
+RTOL = 1e-7   # the compensated form's documented run-to-run bound per pixel
 
 
 def _noalloc(L, parts, n, nside, par, out, accumulate=0, stream=None):
