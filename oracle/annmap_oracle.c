@@ -178,6 +178,76 @@ static double core_correction(const orc_params *p, float x, float y, float z) {
     return r;
 }
 
+/* The same product on unrounded doubles (exact_boost), and its gradient:
+ * d ln(prod) / d pos = sum over the halos containing pos of
+ * -0.9 (pos - c) / r^2.  Membership is decided as in core_func. */
+static double core_correction_exact(const orc_params *p, double x, double y, double z,
+                                    double grad_ln[3]) {
+    double r = 1.0;
+    if (grad_ln) grad_ln[0] = grad_ln[1] = grad_ln[2] = 0.0;
+    for (int i = 0; i < p->n_halos; i++) {
+        const double dx = x - p->halo_x[i], dy = y - p->halo_y[i], dz = z - p->halo_z[i];
+        const double rr = sqrt(dx * dx + dy * dy + dz * dz);
+        const double R = (double)(float)(p->halo_r[i] / (0.73 * 40000.0));
+        if (rr < R && rr > 0) {
+            r *= 0.55 * pow(rr / R, -0.9);
+            if (grad_ln) {
+                grad_ln[0] += -0.9 * dx / (rr * rr);
+                grad_ln[1] += -0.9 * dy / (rr * rr);
+                grad_ln[2] += -0.9 * dz / (rr * rr);
+            }
+        }
+    }
+    return r;
+}
+
+/* src/flux/flux_ann_adiabatic.cpp:17-26: the boost factor f(r) of the
+ * adiabatically contracted host, r = |pos - cpos| * 40000 (kpc/h), and
+ * d ln f / dr. */
+static double adiabatic_factor(double r, double *dlnf_dr) {
+    const double a = 1 + 0.0355872 * r, b = 1 + 0.10888 * pow(r, 0.76);
+    if (dlnf_dr)
+        *dlnf_dr = 1.76 * 0.0355872 / a - 3.34211 * 0.10888 * 0.76 * pow(r, -0.24) / b - 0.13 / r;
+    return (14.6534 * pow(a, 1.76)) / (pow(b, 3.34211) * pow(r, 0.13));
+}
+
+/* d ln(boost) / d pos of the position-dependent flux laws (the adiabatic
+ * factor squared, the halo-core factor squared); zero for the others.  On
+ * the parity path the halo-core terms take the float differences of
+ * halocore.cpp:70-83 (each term then in double). */
+static void boost_grad_ln(const orc_params *p, double x, double y, double z, double g[3]) {
+    g[0] = g[1] = g[2] = 0.0;
+    if (p->flux_model == ORC_FLUX_ADIABATIC) {
+        const double dx = x - p->centerpos[0], dy = y - p->centerpos[1], dz = z - p->centerpos[2];
+        const double rc = sqrt(dx * dx + dy * dy + dz * dz);
+        if (!(rc > 0)) return;
+        double dl;
+        adiabatic_factor(rc * 40000.0, &dl);
+        const double k = 2.0 * dl * 40000.0 / rc;
+        g[0] = k * dx;
+        g[1] = k * dy;
+        g[2] = k * dz;
+    } else if (p->flux_model == ORC_FLUX_CORE_NOSOM) {
+        double gl[3] = {0.0, 0.0, 0.0};
+        if (p->exact_boost) {
+            core_correction_exact(p, x, y, z, gl);
+        } else {
+            const float xf = (float)x, yf = (float)y, zf = (float)z;
+            for (int i = 0; i < p->n_halos; i++) {
+                const float xx = xf - p->halo_x[i], yy = yf - p->halo_y[i], zz = zf - p->halo_z[i];
+                const double rr = sqrt((double)xx * xx + (double)yy * yy + (double)zz * zz);
+                const float R = (float)(p->halo_r[i] / (0.73 * 40000.0));
+                if (rr < R && rr > 0) {
+                    gl[0] += -0.9 * xx / (rr * rr);
+                    gl[1] += -0.9 * yy / (rr * rr);
+                    gl[2] += -0.9 * zz / (rr * rr);
+                }
+            }
+        }
+        for (int k = 0; k < 3; k++) g[k] = 2.0 * gl[k];
+    }
+}
+
 /* getflux of the flux law p->flux_model for one particle at distance d, each
  * in the operation order of its plugin (sigmav only read by the laws that
  * use it). */
@@ -219,7 +289,8 @@ static double orc_flux(const orc_params *p, double mass, double dens, double sig
         return fluxes;
     }
     case ORC_FLUX_CORE_NOSOM: { /* src/flux/flux_ann_core_nosom.cpp:9-17 */
-        double r = core_correction(p, (float)px, (float)py, (float)pz);
+        double r = p->exact_boost ? core_correction_exact(p, px, py, pz, NULL)
+                                  : core_correction(p, (float)px, (float)py, (float)pz);
         return r * r * uf * dens * mass / (4.0 * PI * d * d);
     }
     default: /* src/flux/flux_ann_nosom.cpp:12-23 */
@@ -544,9 +615,10 @@ int orc_adjoint_v(const orc_params *p, const float *mass, const float *dens,
                   const float *hsmooth, const float *x, const float *y, const float *z,
                   const float *sigmav, int64_t n, const double *G, double *grad,
                   double oacc[12]) {
-    /* laws whose flux is rho m (or m) times a factor of sigma v alone over
-       d^2: nosom, somv, somv2, pwave, decay */
-    if (p->flux_model < 0 || p->flux_model > 4) return -2;
+    /* every law: the flux is rho m (or m under decay) over d^2 times a
+       factor of sigma v (somv, somv2, pwave) or of the position (adiabatic,
+       ann_core_nosom), whose log-gradient joins the position gradient */
+    if (p->flux_model < 0 || p->flux_model > 6) return -2;
     orc_hpx hb;
     orc_hpx_init(&hb, p->nside);
     int32_t *list = (int32_t *)malloc(sizeof(int32_t) * (size_t)p->npix);
@@ -604,11 +676,13 @@ int orc_adjoint_v(const orc_params *p, const float *mass, const float *dens,
         double F = fd * rho_f * (double)mass[i];
         double w[3] = {-KV[0], -KV[1], KV[2]}; /* D K V, D = diag(-1,-1,1) */
         double cr = -(2.0 * Gb * F + KT) / d;
+        double gb[3];   /* the boost's own position dependence (not the observer's) */
+        boost_grad_ln(p, (double)x[i], (double)y[i], (double)z[i], gb);
         for (int j = 0; j < 3; j++) {
             double rw = p->rotmatrix[j][0] * w[0] + p->rotmatrix[j][1] * w[1] +
                         p->rotmatrix[j][2] * w[2];
             double gj = cr * uh[j] + rw / d;
-            grad[j * n + i] = gj;
+            grad[j * n + i] = gj + Gb * F * gb[j];
             oacc[j] += gj;
         }
         grad[3 * n + i] = Gb * fd * rho_f;

@@ -87,6 +87,11 @@ typedef struct {
      * line, in file order; not owned) */
     const float *halo_x, *halo_y, *halo_z, *halo_r;
     int n_halos;
+    /* 0: the halo-core factor rounds positions and centres to float as
+     * halocore.cpp does (the parity path).  1: it takes the unrounded
+     * doubles -- the smooth function whose derivative the adjoint returns,
+     * for central differences finer than the float rounding. */
+    int exact_boost;
 } orc_params;
 
 /* Flux laws, in the numbering of the C ABI's dmann_flux. */
@@ -168,9 +173,11 @@ void orc_particle_losses(const orc_params *p, const double *mass, const double *
                          const double *z, int64_t n, const double *G, double *L,
                          uint64_t *sig);
 
-/* grad = [6][n] (x, y, z, m, rho, h); oacc[0..2] = sum_i dL/du_i,
- * oacc[3..11] = dL/drot (row-major).  Returns 0 on success, -2 for a flux
- * law whose flux is not rho m (or m) times a factor of sigma v over d^2. */
+/* grad = [6][n] (x, y, z, m, rho, h); oacc[0..2] = sum_i dL/du_i (u = pos -
+ * opos: the geometric terms only), oacc[3..11] = dL/drot (row-major).  Every
+ * flux law: the adiabatic and ann_core_nosom factors depend on the particle's
+ * position, and d ln(factor) / d pos joins dL/dpos (halo-core membership
+ * held fixed).  Returns 0 on success, -2 for an unknown flux law. */
 int orc_adjoint(const orc_params *p, const float *mass, const float *dens,
                 const float *hsmooth, const float *x, const float *y, const float *z,
                 int64_t n, const double *G, double *grad, double oacc[12]);

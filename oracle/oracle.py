@@ -44,6 +44,7 @@ class OrcParams(C.Structure):
         ("flux_model", C.c_int), ("decay_unit_factor", C.c_double),
         ("halo_x", C.POINTER(C.c_float)), ("halo_y", C.POINTER(C.c_float)),
         ("halo_z", C.POINTER(C.c_float)), ("halo_r", C.POINTER(C.c_float)), ("n_halos", C.c_int),
+        ("exact_boost", C.c_int),
     ]
 
 
@@ -161,11 +162,14 @@ class Healpix:
 # ---------------------------------------------------------------- params
 def make_params(*, nside, obs_pos, centerpos, align_vec, h100=0.73, Omega_M=0.238,
                 Lbox_in_Mpc=0.001, mass_to_Msun=1.0, particle_masses=(0.0,),
-                redshift=0.0, flux_model=0, halos=None) -> OrcParams:
+                redshift=0.0, flux_model=0, halos=None, exact_boost=False) -> OrcParams:
     """halos: optional (x, y, z, radius) arrays of the ann_core_nosom law's
-    halo table (kept alive on the returned object)."""
+    halo table (kept alive on the returned object).  exact_boost: the halo-
+    core factor on unrounded positions (for central differences; the
+    reference rounds them to float)."""
     p = OrcParams()
     p.flux_model = int(flux_model)
+    p.exact_boost = int(bool(exact_boost))
     if halos is not None:
         arrs = [np.ascontiguousarray(a, dtype=np.float32) for a in halos]
         p._halos = arrs

@@ -121,15 +121,60 @@ def test_oracle_adjoint_decay_law(decay_case):
     assert np.sum(m * grad[3]) == pytest.approx(L, rel=1e-10)
 
 
-def test_oracle_adjoint_rejects_position_dependent_laws():
-    """adiabatic and ann_core_nosom boost the flux by a function of the
-    particle's position, which the adjoint does not differentiate."""
-    P, parts, p0 = make_case(200, 32, seed=3)
-    for law in (5, 6):
-        p = O.make_params(nside=32, obs_pos=P.obs_pos, centerpos=P.centerpos,
-                          align_vec=P.align_vec, particle_masses=(P.particle_mass,), flux_model=law)
-        with pytest.raises(RuntimeError):
-            O.adjoint(p, parts, np.ones(12 * 32 * 32))
+def core_halos(P, n=40, seed=9):
+    """A halo-core table (x, y, z, radius in the table's units) whose cores
+    hold some of P's particles: centres 1 kpc from particles (never on one:
+    at r = 0 the reference's factor drops back to 1), core radii of a few kpc
+    (the core radius is radius / (0.73 * 40000) box units)."""
+    rng = np.random.default_rng(seed)
+    idx = rng.choice(len(P), n, replace=False)
+    off = rng.standard_normal((n, 3))
+    off /= np.linalg.norm(off, axis=1)[:, None]
+    rad = rng.uniform(2.0, 8.0, n) * 0.73 * 40000.0
+    return (P.x[idx] + off[:, 0], P.y[idx] + off[:, 1], P.z[idx] + off[:, 2], rad.astype(np.float32))
+
+
+@pytest.mark.parametrize("law", [5, 6], ids=["adiabatic", "core"])
+def test_oracle_adjoint_position_dependent_laws(law):
+    """adiabatic (flux x f(r)^2, r from the halo centre) and ann_core_nosom
+    (flux x the halo-core factor squared): the boost's own position gradient
+    joins dL/dpos (the observer sums exclude it).  Central differences use
+    the core factor on unrounded positions (exact_boost), the smooth
+    function the adjoint differentiates."""
+    P, parts, p0 = make_case(2000, 128, seed=50 + law, single_frac=0.2, skipped=20)
+    halos = core_halos(P) if law == 6 else None
+    kw = dict(nside=128, obs_pos=P.obs_pos, centerpos=P.centerpos, align_vec=P.align_vec,
+              particle_masses=(P.particle_mass,), flux_model=law, halos=halos)
+    p = O.make_params(exact_boost=True, **kw)
+    mp, _, _ = O.render(p, parts)
+    target, _, _ = O.render(p, __import__("adjoint_cases").jittered(P))
+    _, G = loss_grad(mp, target)
+    grad, oacc = O.adjoint(p, parts, G)
+    res = fd_check(p, parts, G, grad)
+    for k in FIELDS:
+        err, n_ok = res[k]
+        assert n_ok > 1600, (k, n_ok)
+        assert err < 1e-6, (k, err)
+    L = float(np.dot(G, mp))
+    m, rho = (parts[k].astype(np.float64) for k in ("m", "rho"))
+    assert np.sum(m * grad[3]) == pytest.approx(L, rel=1e-10)
+    assert np.sum(rho * grad[4]) == pytest.approx(L, rel=1e-10)
+    # the boost term is present: without it the homogeneity identity
+    # sum(u . dL/du) + sum(h dL/dh) = -2 L would hold; with it, it does not
+    o = np.array(p.obs_pos[:])
+    u = np.stack([parts[k].astype(np.float64) - o[i] for i, k in enumerate(("x", "y", "z"))])
+    h = parts["h"].astype(np.float64)
+    assert abs(np.sum(u * grad[:3]) + np.sum(h * grad[5]) + 2 * L) > 1e-6 * abs(L)
+    # the observer gradient excludes the boost term (it moves with the
+    # particle, not with the observer)
+    fd, keep = observer_fd(p, parts, G)
+    sub = {k: np.asarray(parts[k])[keep] for k in FIELDS}
+    _, oa = O.adjoint(p, sub, G)
+    go = O.observer_grad(p, oa)
+    assert np.linalg.norm(go - fd) < 1e-6 * np.linalg.norm(fd)
+    if law == 6:   # the parity (float-rounded) core factor moves the gradient by ~1e-7
+        g_r, _ = O.adjoint(O.make_params(**kw), parts, G)
+        assert np.linalg.norm(g_r - grad) < 1e-5 * np.linalg.norm(grad)
 
 
 @pytest.mark.parametrize("law", [1, 2, 3], ids=["somv", "somv2", "pwave"])
