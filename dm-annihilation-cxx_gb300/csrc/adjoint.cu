@@ -198,10 +198,13 @@ constexpr int kWPB = 8, kRCHW = 64;
 
 cudaError_t launch_adjoint(const DiscArgs &d, const Particles &p, const signed char *cls,
                            const double *gmap, float *gmap32, double *grad, double *oacc,
-                           int precision, int num_sms, cudaStream_t s) {
+                           int precision, int num_sms, cudaStream_t s, const double *core_corr,
+                           const double *core_gln) {
     AdjArgs a;
     a.d = d;
     a.p = p;
+    a.core_corr = core_corr;
+    a.core_gln = core_gln;
     a.cls = cls;
     a.gmap = gmap;
     a.gmap32 = gmap32;

@@ -56,6 +56,7 @@ struct dmann_ctx {
     // workspace
     DevBuf in[7], theta, phi, ar, flux, cpix, key, queue, hist, ctr, fsum, acc, map;
     DevBuf cls, oacc, grad;   // the adjoint's class array, observer sums, staged gradient
+    DevBuf core_gln;          // the adjoint's d ln(halo-core factor) / d pos, [3][n]
     DevBuf chdr;              // the compensated form's disc headers, one per queue slot
     // halo cores of the ann_core_nosom law (dmann_set_halo_cores)
     DevBuf halo_f, halo_cells, corr;
@@ -305,7 +306,7 @@ void dmann_destroy(dmann_ctx *ctx) {
                       &ctx->theta, &ctx->phi, &ctx->ar, &ctx->flux, &ctx->cpix, &ctx->key,
                       &ctx->queue, &ctx->hist, &ctx->ctr, &ctx->fsum, &ctx->acc, &ctx->map,
                       &ctx->cls, &ctx->oacc, &ctx->grad, &ctx->halo_f, &ctx->halo_cells,
-                      &ctx->corr, &ctx->chdr};
+                      &ctx->corr, &ctx->chdr, &ctx->core_gln};
     for (DevBuf *b : bufs)
         if (b->p) cudaFree(b->p);
     for (auto &kv : ctx->rings) {
@@ -672,7 +673,7 @@ dmann_status dmann_map_add_v(dmann_ctx *ctx, const float *x, const float *y, con
     if (ctx->flux_model == DMANN_FLUX_ANN_CORE_NOSOM) {
         if (!ctx->have_halos) return fail(ctx, DMANN_ERR_STATE, "halo cores not set (dmann_set_halo_cores)");
         if ((st = ensure(ctx, ctx->corr, 8 * N)) != DMANN_OK) return st;
-        CK(launch_halo_core(ctx->halo, pa.p, (double *)ctx->corr.p, s));
+        CK(launch_halo_core(ctx->halo, pa.p, (double *)ctx->corr.p, nullptr, s));
         pa.core_corr = (const double *)ctx->corr.p;
         ctx->launches++;
     }
@@ -892,7 +893,7 @@ dmann_status dmann_render_batch(dmann_ctx *ctx, const float *x, const float *y, 
         if (!ctx->have_halos) return fail(ctx, DMANN_ERR_STATE, "halo cores not set (dmann_set_halo_cores)");
         if ((st = ensure(ctx, ctx->corr, 8 * n1)) != DMANN_OK) return st;
         Particles pp = {dev[0], dev[1], dev[2], dev[3], dev[4], dev[5], (int)N};
-        CK(launch_halo_core(ctx->halo, pp, (double *)ctx->corr.p, s));
+        CK(launch_halo_core(ctx->halo, pp, (double *)ctx->corr.p, nullptr, s));
     }
     std::vector<char> on_dev(n_obs);
     bool all_dev = true;
@@ -959,6 +960,14 @@ dmann_status dmann_adjoint(dmann_ctx *ctx, const float *x, const float *y, const
                            const float *m, const float *rho, const float *h, int64_t n, int nside,
                            int precision, const double *grad_map, double *grad,
                            double grad_opos[3]) {
+    return dmann_adjoint_v(ctx, x, y, z, m, rho, h, nullptr, n, nside, precision, grad_map, grad,
+                           grad_opos);
+}
+
+dmann_status dmann_adjoint_v(dmann_ctx *ctx, const float *x, const float *y, const float *z,
+                             const float *m, const float *rho, const float *h, const float *sigmav,
+                             int64_t n, int nside, int precision, const double *grad_map,
+                             double *grad, double grad_opos[3]) {
     if (!ctx) return DMANN_ERR_INVALID;
     if (precision != DMANN_PLAIN_F64 && precision != DMANN_COMP_F32)
         return fail(ctx, DMANN_ERR_INVALID, "unknown precision form");
@@ -968,10 +977,12 @@ dmann_status dmann_adjoint(dmann_ctx *ctx, const float *x, const float *y, const
     if (!ctx->have_frame) return fail(ctx, DMANN_ERR_STATE, "observer frame not set");
     if (!ctx->have_units) return fail(ctx, DMANN_ERR_STATE, "units not set");
     if (ctx->in_map) return fail(ctx, DMANN_ERR_STATE, map_open_msg);
-    if (ctx->flux_model != DMANN_FLUX_ANN_NOSOM && ctx->flux_model != DMANN_FLUX_DECAY)
-        return fail(ctx, DMANN_ERR_INVALID, "the adjoint supports the nosom and decay flux laws only");
     dmann_status st = check_particles(ctx, x, y, z, m, rho, h, n);
     if (st != DMANN_OK) return st;
+    if (n > 0 && !sigmav && law_needs_sigmav(ctx->flux_model))
+        return fail(ctx, DMANN_ERR_INVALID, "this flux law needs the velocity dispersion (dmann_adjoint_v)");
+    const bool core = ctx->flux_model == DMANN_FLUX_ANN_CORE_NOSOM;
+    if (core && !ctx->have_halos) return fail(ctx, DMANN_ERR_STATE, "halo cores not set (dmann_set_halo_cores)");
     CK(cudaSetDevice(ctx->device));
     if ((st = collect_stats(ctx)) != DMANN_OK) return st;
     cudaStream_t s = ctx->stream;
@@ -986,13 +997,16 @@ dmann_status dmann_adjoint(dmann_ctx *ctx, const float *x, const float *y, const
         (st = ensure(ctx, ctx->hist, 4 * (size_t)kKeys)) || (st = ensure(ctx, ctx->ctr, 8 * C_COUNT)) ||
         (st = ensure(ctx, ctx->fsum, 8)) || (st = ensure(ctx, ctx->oacc, 8 * 12)))
         return st;
+    if (core && ((st = ensure(ctx, ctx->corr, 8 * n1)) || (st = ensure(ctx, ctx->core_gln, 24 * n1))))
+        return st;
     if (precision == DMANN_COMP_F32) {
         if ((st = ensure(ctx, ctx->acc, 4 * P)) != DMANN_OK) return st;
         reserve_headers(ctx, n1);
     }
-    const float *src[6] = {x, y, z, m, rho, h};
-    const float *dev[6];
-    for (int k = 0; k < 6; k++) {
+    const float *src[7] = {x, y, z, m, rho, h, law_needs_sigmav(ctx->flux_model) ? sigmav : nullptr};
+    const float *dev[7] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    for (int k = 0; k < 7; k++) {
+        if (!src[k]) continue;
         if (N == 0 || is_device_ptr(src[k])) {
             dev[k] = src[k];
         } else {
@@ -1022,7 +1036,7 @@ dmann_status dmann_adjoint(dmann_ctx *ctx, const float *x, const float *y, const
     CK(cudaMemsetAsync(ctx->oacc.p, 0, 8 * 12, s));
     CK(cudaMemsetAsync(ctx->hist.p, 0, 4 * (size_t)kKeys, s));
     PrepArgs pa;
-    pa.p = {dev[0], dev[1], dev[2], dev[3], dev[4], dev[5], (int)N};
+    pa.p = {dev[0], dev[1], dev[2], dev[3], dev[4], dev[5], (int)N, dev[6]};
     pa.f = f;
     pa.g = g;
     pa.out = {(double *)ctx->theta.p, (double *)ctx->phi.p, (double *)ctx->ar.p,
@@ -1036,6 +1050,10 @@ dmann_status dmann_adjoint(dmann_ctx *ctx, const float *x, const float *y, const
     pa.block_bucket_min = bmin;
     pa.deposit_singles = 0;
     pa.core_corr = nullptr;
+    if (core) {   // the law's factor and its position gradient
+        CK(launch_halo_core(ctx->halo, pa.p, (double *)ctx->corr.p, (double *)ctx->core_gln.p, s));
+        pa.core_corr = (const double *)ctx->corr.p;
+    }
     CK(launch_prep(pa, s));
     CK(launch_scan(pa.hist, pa.ctr, bmin, s));
     CK(launch_scatter(pa, (int *)ctx->queue.p, s));
@@ -1054,7 +1072,8 @@ dmann_status dmann_adjoint(dmann_ctx *ctx, const float *x, const float *y, const
     if (precision == DMANN_COMP_F32) da.chdr = headers_for(ctx, n1);
     CK(cudaEventRecord(ctx->evd0, s));
     CK(launch_adjoint(da, pa.p, pa.out.cls, dgmap, (float *)ctx->acc.p, dgrad, (double *)ctx->oacc.p,
-                      precision, ctx->num_sms, s));
+                      precision, ctx->num_sms, s, core ? (const double *)ctx->corr.p : nullptr,
+                      core ? (const double *)ctx->core_gln.p : nullptr));
     CK(cudaEventRecord(ctx->evd1, s));
     CK(cudaEventRecord(ctx->evdm, s));
     CK(cudaEventRecord(ctx->ev1, s));

@@ -14,18 +14,21 @@
 // FP32 with a margin and only candidates take the reference's FP64
 // expression, which decides membership and gives the factor; the factors of
 // a particle's halos multiply in grid order instead of file order (the
-// product differs in the last bits only).
+// product differs in the last bits only).  For the adjoint the kernel also
+// returns d ln r / d pos = sum over the particle's halos of
+// -0.9 (pos - c_h) / d_h^2 (membership held fixed).
 #include "kernels.cuh"
 
 namespace dmann {
 
 namespace {
 
-__global__ void __launch_bounds__(256) k_halo_core(HaloGrid g, Particles p, double *corr) {
+__global__ void __launch_bounds__(256) k_halo_core(HaloGrid g, Particles p, double *corr, double *gln) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= p.n) return;
     const float x = p.x[i], y = p.y[i], z = p.z[i];
     double r = 1.0;
+    double gx = 0.0, gy = 0.0, gz = 0.0;   // d ln r / d pos: sum of -0.9 (pos - c) / d^2
     const float fx = (x - g.ox) * g.inv_cell, fy = (y - g.oy) * g.inv_cell, fz = (z - g.oz) * g.inv_cell;
     if (fx >= 0.0f && fy >= 0.0f && fz >= 0.0f && fx < (float)g.nx && fy < (float)g.ny && fz < (float)g.nz) {
         const int cx = (int)fx, cy = (int)fy, cz = (int)fz;
@@ -41,18 +44,30 @@ __global__ void __launch_bounds__(256) k_halo_core(HaloGrid g, Particles p, doub
                     if (s32 > rad * rad * 1.0001f) continue;   // clearly outside
                     const double d = sqrt((double)xx * (double)xx + (double)yy * (double)yy +
                                           (double)zz * (double)zz);
-                    if (d < (double)rad && d > 0) r *= 0.55 * pow(d / (double)rad, -0.9);
+                    if (d < (double)rad && d > 0) {
+                        r *= 0.55 * pow(d / (double)rad, -0.9);
+                        const double k = -0.9 / (d * d);
+                        gx += k * (double)xx;
+                        gy += k * (double)yy;
+                        gz += k * (double)zz;
+                    }
                 }
             }
     }
     corr[i] = r;
+    if (gln) {
+        gln[i] = gx;
+        gln[(size_t)p.n + i] = gy;
+        gln[2 * (size_t)p.n + i] = gz;
+    }
 }
 
 }  // namespace
 
-cudaError_t launch_halo_core(const HaloGrid &g, const Particles &p, double *corr, cudaStream_t s) {
+cudaError_t launch_halo_core(const HaloGrid &g, const Particles &p, double *corr, double *grad_ln,
+                             cudaStream_t s) {
     if (p.n <= 0) return cudaSuccess;
-    k_halo_core<<<(p.n + 255) / 256, 256, 0, s>>>(g, p, corr);
+    k_halo_core<<<(p.n + 255) / 256, 256, 0, s>>>(g, p, corr, grad_ln);
     return cudaGetLastError();
 }
 

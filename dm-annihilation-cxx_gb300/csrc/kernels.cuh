@@ -97,8 +97,10 @@ cudaError_t launch_scan(int *hist, long long *ctr, int block_bucket_min, cudaStr
 cudaError_t launch_scatter(const PrepArgs &a, int *queue, cudaStream_t s);
 cudaError_t launch_finalize(const Accum &acc, int precision, int npix, double dOmega,
                             double scale, double *out, int accumulate, cudaStream_t s);
-// halocore.cu: corr[i] = the halo-core factor r of particle i
-cudaError_t launch_halo_core(const HaloGrid &g, const Particles &p, double *corr, cudaStream_t s);
+// halocore.cu: corr[i] = the halo-core factor r of particle i; grad_ln
+// (optional, [3][n]) = d ln r / d pos
+cudaError_t launch_halo_core(const HaloGrid &g, const Particles &p, double *corr, double *grad_ln,
+                             cudaStream_t s);
 // disc_plain.cu / disc_comp.cu
 // Launch the block-per-particle kernel, record `mid` (if not null), then the
 // warp-per-particle kernel.
@@ -117,6 +119,7 @@ size_t comp_hdr_bytes();
 // compensated form's FP32 weights; gmap32 receives gmap rounded, npix floats).
 cudaError_t launch_adjoint(const DiscArgs &d, const Particles &p, const signed char *cls,
                            const double *gmap, float *gmap32, double *grad, double *oacc,
-                           int precision, int num_sms, cudaStream_t s);
+                           int precision, int num_sms, cudaStream_t s,
+                           const double *core_corr = nullptr, const double *core_gln = nullptr);
 
 }  // namespace dmann

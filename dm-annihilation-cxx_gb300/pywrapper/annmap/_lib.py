@@ -78,6 +78,8 @@ SIGNATURES = {
     "dmann_render_batch": (C.c_int, [_P, _P, _P, _P, _P, _P, _P, C.c_int64, C.c_int, _D3, _D3,
                                      C.POINTER(C.c_int), C.c_int, C.POINTER(C.c_void_p)]),
     "dmann_adjoint": (C.c_int, [_P, _P, _P, _P, _P, _P, _P, C.c_int64, C.c_int, C.c_int, _P, _P, _D3]),
+    "dmann_adjoint_v": (C.c_int, [_P, _P, _P, _P, _P, _P, _P, _P, C.c_int64, C.c_int, C.c_int, _P, _P,
+                                  _D3]),
     "dmann_measure_l2_red": (C.c_int, [C.c_int, C.c_int, C.c_int64, C.c_int, _D3]),
     "dmann_observer_rotation": (C.c_int, [_D3, _D3, _D3, _D3, _D3]),
     "dmann_observer_rotation_jacobian": (C.c_int, [_D3, _D3, _D3, _D3]),

@@ -228,14 +228,18 @@ class Renderer:
 
     def adjoint(self, parts: dict, nside: int, grad_map, out=None, precision: int = PLAIN_F64):
         """Gradient of L = sum_p grad_map[p] * map[p] (the map of ``render``
-        for this frame and these units) with respect to the particle inputs and
-        the observer position; precision PLAIN_F64 recomputes the weights in
-        FP64, COMP_F32 with the compensated form's FP32 weights (faster).  Returns (grad, grad_opos): grad is
-        [6, n] float64 (rows x, y, z, m, rho, h; a CUDA tensor when the inputs
-        are CUDA tensors, else numpy), grad_opos a length-3 numpy array."""
+        for this frame, these units and this flux law) with respect to the
+        particle inputs and the observer position; precision PLAIN_F64
+        recomputes the weights in FP64, COMP_F32 with the compensated form's
+        FP32 weights (faster).  The velocity dispersion "sigmav" (the somv,
+        somv2 and pwave laws) is an input, not differentiated.  Returns
+        (grad, grad_opos): grad is [6, n] float64 (rows x, y, z, m, rho, h; a
+        CUDA tensor when the inputs are CUDA tensors, else numpy), grad_opos a
+        length-3 numpy array."""
         arrays = [parts[f] for f in FIELDS]
         n = len(arrays[0])
-        if any(len(a) != n for a in arrays):
+        sv = parts.get("sigmav")
+        if any(len(a) != n for a in arrays) or (sv is not None and len(sv) != n):
             raise ValueError("particle arrays differ in length")
         npix = 12 * int(nside) * int(nside)
         if len(grad_map) != npix:
@@ -248,13 +252,14 @@ class Renderer:
                 out = torch.empty((6, n), dtype=torch.float64, device=arrays[0].device)
             else:
                 out = np.zeros((6, n), dtype=np.float64)
-        self._use_torch_stream(arrays + [grad_map, out])
+        self._use_torch_stream(arrays + [grad_map, out] + ([sv] if sv is not None else []))
         ptrs = [self._ptr(a, np.float32) for a in arrays]
+        svp = self._ptr(sv, np.float32) if sv is not None else None
         gm = self._ptr(grad_map, np.float64)
         optr = C.c_void_p(out.data_ptr() if _is_torch(out) else out.ctypes.data)
         go = (C.c_double * 3)()
-        self._check(self.L.dmann_adjoint(self.ctx, *ptrs, int(n), int(nside), int(precision), gm,
-                                         optr, go))
+        self._check(self.L.dmann_adjoint_v(self.ctx, *ptrs, svp, int(n), int(nside), int(precision),
+                                           gm, optr, go))
         self._keep = []
         return out, np.array(go[:])
 

@@ -238,9 +238,13 @@ dmann_status dmann_render_batch(dmann_ctx *ctx, const float *x, const float *y,
                                 double *const *maps);
 
 /* ---- differentiation ---- */
-/* Adjoint of dmann_render (no reference counterpart), for the nosom and
- * decay flux laws (their flux is rho m, or m, times a constant over d^2;
- * under decay dL/drho = 0); other laws give DMANN_ERR_INVALID.
+/* Adjoint of dmann_render (no reference counterpart), for every flux law:
+ * the flux is rho m (m under decay, where dL/drho = 0) over d^2 times the
+ * law's factor -- of the velocity dispersion for somv, somv2 and pwave
+ * (sigma v is an input, not differentiated: use dmann_adjoint_v), of the
+ * particle's position for adiabatic and ann_core_nosom (that factor's own
+ * position derivative joins dL/dpos but not dL/dopos; halo-core membership
+ * is held fixed).
  * grad_map[p] = dL/dmap[p] for a scalar loss L of the map dmann_render
  * returns for these particles, this nside and the context's frame and units
  * (12*nside^2 doubles, host or device).  Writes dL/d(particle inputs) into
@@ -263,6 +267,13 @@ dmann_status dmann_adjoint(dmann_ctx *ctx, const float *x, const float *y,
                            const float *h, int64_t n, int nside, int precision,
                            const double *grad_map, double *grad,
                            double grad_opos[3]);
+/* dmann_adjoint with each particle's velocity dispersion (as dmann_render_v);
+ * the somv, somv2 and pwave laws need it, the others accept NULL. */
+dmann_status dmann_adjoint_v(dmann_ctx *ctx, const float *x, const float *y,
+                             const float *z, const float *m, const float *rho,
+                             const float *h, const float *sigmav, int64_t n,
+                             int nside, int precision, const double *grad_map,
+                             double *grad, double grad_opos[3]);
 
 /* Statistics of the last completed map (synchronises the stream). */
 dmann_status dmann_get_stats(const dmann_ctx *ctx, dmann_stats *out);

@@ -12,7 +12,8 @@ Function over it) against its references.
     finite-difference Jacobian on the oracle side) <= 1e-8 of the oracle's,
     and <= 1e-6 of central differences of the summed loss;
   * the decay law (flux ~ m / d^2): dL/drho = 0 and the other fields as
-    the oracle's; laws with other dependences are refused;
+    the oracle's; somv, somv2, pwave, adiabatic and ann_core_nosom against
+    the oracle's adjoint of the same law;
   * at the full adjoint workload (4,194,304 particles, Nside 512) the
     size-independent Euler identities of the map: it is linear in m and in
     rho, and homogeneous of degree -2 in (pos - opos, h), so
@@ -223,7 +224,7 @@ def test_adjoint_decay_law_matches_oracle(prec):
     assert np.linalg.norm(gopos - go_ref) <= TOL_OBS[prec] * np.linalg.norm(go_ref)
 
 
-def test_adjoint_rejects_laws_with_other_dependences():
+def test_adjoint_sigma_v_law_needs_the_dispersion():
     P, parts, p = make_case(500, 32, seed=31)
     r = annmap.Renderer(0)
     r.set_observer(P.obs_pos, P.centerpos, P.align_vec)
@@ -231,6 +232,46 @@ def test_adjoint_rejects_laws_with_other_dependences():
     with pytest.raises(annmap.DmannError):
         r.adjoint(parts, 32, np.ones(12 * 32 * 32))
     r.close()
+
+
+@pytest.mark.parametrize("prec", [PLAIN, COMP], ids=["plain", "comp"])
+@pytest.mark.parametrize("law", [1, 2, 3, 5, 6], ids=["somv", "somv2", "pwave", "adiabatic", "core"])
+def test_adjoint_other_laws_match_oracle(law, prec):
+    """somv, somv2, pwave (a factor of the velocity dispersion, an input),
+    adiabatic and ann_core_nosom (a factor of the position, whose gradient
+    joins dL/dpos): the GPU adjoint against the oracle's FP64 adjoint of the
+    same law (the oracle's own adjoint is checked against central
+    differences in test_adjoint_cpu.py)."""
+    from test_adjoint_cpu import core_halos
+    P, parts, p0 = make_case(20000, 128, seed=60 + law, single_frac=0.2, skipped=100)
+    halos = core_halos(P, n=400) if law == 6 else None
+    p = O.make_params(nside=128, obs_pos=P.obs_pos, centerpos=P.centerpos, align_vec=P.align_vec,
+                      particle_masses=(P.particle_mass,), flux_model=law, halos=halos)
+    if law in (1, 2, 3):
+        kms = 1e5 / p.velocity_to_cgs
+        sv = np.random.default_rng(law).uniform(0.2, 12.0, len(P)) * kms
+        parts = dict(parts, sigmav=sv.astype(np.float32))
+    r = annmap.Renderer(0)
+    r.set_observer(P.obs_pos, P.centerpos, P.align_vec)
+    r.set_units(p.unit_factor, p.hires_threshold, flux_model=law)
+    r.set_flux_params(p.velocity_to_cgs, P.centerpos)
+    if halos is not None:
+        r.set_halo_cores(*halos)
+    mp = r.render(parts, 128, PLAIN)
+    ref_map, _, _ = O.render(p, parts)
+    assert _normwise(mp, ref_map) <= 1e-12
+    jit = jittered(P)
+    if "sigmav" in parts:
+        jit["sigmav"] = parts["sigmav"]
+    target = r.render(jit, 128, PLAIN)
+    _, G = loss_grad(mp, target)
+    grad, gopos = r.adjoint(parts, 128, G, precision=prec)
+    r.close()
+    ref, oacc = O.adjoint(p, parts, G)
+    for k, f in enumerate(FIELDS):
+        assert _normwise(grad[k], ref[k]) <= TOL_ORACLE[prec], (f, _normwise(grad[k], ref[k]))
+    go_ref = O.observer_grad(p, oacc)
+    assert np.linalg.norm(gopos - go_ref) <= TOL_OBS[prec] * np.linalg.norm(go_ref)
 
 
 def test_sky_map_autograd_decay_law():
