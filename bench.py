@@ -34,7 +34,6 @@ import numpy as np  # noqa: E402
 METRIC = "particles/s at Nside 2048: comp-FP32 vs plain GPU form; px err vs FP64"
 UNIT = "particles/s"
 WORKLOAD = "nfw16m_sub100_ns2048"
-KERNELS_PER_STEP = 7  # prep, key scan, queue scatter, disc headers, disc (block), disc (warp), finalize
 
 
 def parse():
@@ -198,36 +197,72 @@ def cpu_oracle_run(P, nside, seconds, threads=None):
     mp, st, tot = O.render(o, sub.as_dict(), nthreads=threads)
     dt = time.perf_counter() - t0
     return {"value": n / dt, "unit": UNIT, "cores": threads, "seconds": dt, "particles": n,
-            "deposits": st["deposits"]}, sub, mp, tot
+            "deposits": st["deposits"], "deposits_per_s": st["deposits"] / dt}, sub, mp, tot
+
+
+def bench_config(args, n, nside):
+    """The workload description both arms print (identical in the two lines)."""
+    return {"workload": args.workload + (f" (first {n} particles)" if args.subset else ""),
+            "particles": n, "nside": nside,
+            "l2": f"no flush: inputs {24 * n / 1e6:.0f} MB + map/planes "
+                  f"{16 * 12 * nside * nside / 1e6:.0f} MB > 126 MB L2"}
 
 
 def run_reference(args, ws, rank):
     """The reference arm: the CPU restatement of the reference's own map path
-    (src/genmap.cpp) timed on this host's cores on the same workload."""
+    (src/genmap.cpp) on every host thread, on the same workload.  Each step
+    renders a different slice of the shuffled (hence i.i.d.) particle set,
+    sized so that the timed steps take about 60 s together; particles/s and
+    deposits/s are totals over the timed slices, and ms_per_step is the time
+    the whole set would take at that rate (an extrapolation)."""
     if rank != 0:
         return
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import oracle as O
     from annmap import synth
     P, nside = synth.workload(args.workload, scale=args.scale)
     if args.subset:
         P = P.subset(slice(0, args.subset))
+    n = len(P)
     threads = os.cpu_count() or 1
-    per_step = max(2.0, min(20.0, 150.0 / max(1, args.steps + args.warmup)))
-    vals = []
-    info = None
+    o = O.make_params(nside=nside, obs_pos=P.obs_pos, centerpos=P.centerpos, align_vec=P.align_vec,
+                      particle_masses=(P.particle_mass,))
+    # a calibration slice, then slices of about `per_step` seconds (warm-up
+    # steps a tenth of that)
+    per_step = min(20.0, max(3.0, 60.0 / max(1, args.steps)))
+    k0 = min(n, 64 * threads)
+    t0 = time.perf_counter()
+    O.render(o, P.subset(slice(0, k0)).as_dict(), nthreads=threads, finalize=False)
+    rate0 = k0 / max(time.perf_counter() - t0, 1e-3)
+    pos = k0
+    parts = dep = secs = 0.0
     for i in range(args.warmup + args.steps):
-        info, _, _, _ = cpu_oracle_run(P.subset(slice(i * 0, None)), nside, per_step, threads)
+        k = max(threads, int(rate0 * per_step * (0.1 if i < args.warmup else 1.0)))
+        k = min(k, n)
+        if pos + k > n:
+            pos = 0
+        sub = P.subset(slice(pos, pos + k))
+        pos += k
+        t0 = time.perf_counter()
+        _, st, _ = O.render(o, sub.as_dict(), nthreads=threads, finalize=False)
+        dt = time.perf_counter() - t0
         if i >= args.warmup:
-            vals.append(info["value"])
-    v = statistics.median(vals)
+            parts += k
+            dep += st["deposits"]
+            secs += dt
+    v = parts / secs
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * len(P) / v,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * n / v,
+            "ms_per_step_basis": "extrapolated: whole-set particles / the timed slices' rate",
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (seeded NFW host + subhalos)",
-            "config": {"workload": args.workload, "particles": len(P), "nside": nside,
-                       "form": "reference CPU map path (FP64), restated"},
+            "config": bench_config(args, n, nside),
+            "form": "reference CPU map path (FP64), restated; all host threads",
+            "deposits_per_s": dep / secs, "timed_seconds": secs,
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
-                             "sample": f"{info['particles']} of {len(P)} particles per step "
-                                       f"(shuffled prefix, i.i.d.), all {threads} host threads"},
+                             "sample": f"{int(parts)} of {n} particles over {args.steps} timed steps, "
+                                       f"a different slice of the shuffled (i.i.d.) set per step, "
+                                       f"{secs:.1f} s on all {threads} host threads"},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -275,11 +310,13 @@ def run_gb300(args, ws, rank, local):
         barrier(ws)
         torch.cuda.synchronize()
         e0.record(stream)
+        launches = 0
         for _ in range(args.steps):
             r.render(dparts, nside, annmap.COMP_F32, out=dmap)
             step_stats = r.stats()
             disc_ms.append(step_stats["disc_ms"])
             step_ms.append(step_stats["kernel_ms"])
+            launches += step_stats["launches"]
         e1.record(stream)
         torch.cuda.synchronize()
         barrier(ws)
@@ -293,15 +330,11 @@ def run_gb300(args, ws, rank, local):
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded NFW host + 100 subhalos; reference data unavailable)",
-            "config": {"workload": args.workload + (f" (first {n} particles)" if args.subset else ""),
-                       "particles": n, "nside": nside,
-                       "form": "compensated FP32 (FP64 geometry, FP32 weights, two-float sums)",
-                       "parallelism": f"replicas x{ws}",
-                       "l2": f"no flush: inputs {24 * n / 1e6:.0f} MB + map/planes "
-                             f"{16 * npix / 1e6:.0f} MB > 126 MB L2",
-                       "tuning": dict(tuned["best"], autotune_s=round(tuned["seconds"], 2),
-                                      cached=tuned["cached"])},
-            "clocks": clocks, "gpu_launches": KERNELS_PER_STEP * args.steps,
+            "config": bench_config(args, n, nside),
+            "form": "compensated FP32 (FP64 geometry, FP32 weights, two-float sums)",
+            "parallelism": f"replicas x{ws}",
+            "tuning": dict(tuned["best"], autotune_s=round(tuned["seconds"], 2), cached=tuned["cached"]),
+            "clocks": clocks, "gpu_launches": launches,
             "deposits_per_step": step_stats["deposits"],
             "deposits_per_s": step_stats["deposits"] / (ms / 1e3),
             # the map's total (sum x dOmega) against the kept particles' flux
@@ -340,26 +373,37 @@ def run_gb300(args, ws, rank, local):
 
     if not args.no_extras and rank == 0:
         # plain FP64 form on a prefix (the plain form is FP64-throughput bound)
+        # (the shuffled set's prefix is an i.i.d. sample, so particles/s carries
+        # over to the whole set; both forms are timed with CUDA events on it)
         k = max(1024, int(n * args.plain_scale))
         sub = {kk: v[:k] for kk, v in dparts.items()}
         pmap = torch.zeros_like(dmap)
         cmap = torch.zeros_like(dmap)
-        r.render(sub, nside, annmap.PLAIN_F64, out=pmap)
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        r.render(sub, nside, annmap.PLAIN_F64, out=pmap)
-        torch.cuda.synchronize()
-        tp = time.perf_counter() - t0
-        pst = r.stats()
-        r.render(sub, nside, annmap.COMP_F32, out=cmap)
-        cst = r.stats()
-        torch.cuda.synchronize()
+
+        def timed(prec, out, reps=3):
+            r.render(sub, nside, prec, out=out)
+            t = []
+            for _ in range(reps):
+                a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                a0.record(stream)
+                r.render(sub, nside, prec, out=out)
+                a1.record(stream)
+                torch.cuda.synchronize()
+                t.append(a0.elapsed_time(a1))
+            return statistics.median(t), r.stats()
+
+        tp, pst = timed(annmap.PLAIN_F64, pmap)
+        tc, cst = timed(annmap.COMP_F32, cmap)
         pm, cm = pmap.cpu().numpy(), cmap.cpu().numpy()
         med, mx = rel_err(cm, pm)
-        plain_value = k / tp
+        plain_value = k / (tp / 1e3)
         line["plain_form"] = {"value": plain_value, "unit": UNIT, "particles": k,
-                              "ms_per_step": tp * 1e3, "disc_ms": pst["disc_ms"]}
-        line["speedup_vs_plain"] = value / ws / plain_value
+                              "ms_per_step": tp, "deposits_per_s": pst["deposits"] / (tp / 1e3),
+                              "timing": f"CUDA events, median of 3 renders of the first {k} particles "
+                                        f"(1/{round(n / k)} of the set, i.i.d.)",
+                              "comp_same_particles": {"value": k / (tc / 1e3), "ms_per_step": tc}}
+        # the two forms on the same particles
+        line["speedup_vs_plain"] = tp / tc
         line["px_err"] = {"vs": "GPU plain FP64 form, same particles", "particles": k,
                           "median": med, "max": mx, "floor": "pixels > 1e-6 max",
                           "total_flux_rel": abs(cm.sum() - pm.sum()) / pm.sum(),
