@@ -29,7 +29,7 @@ COMMON = ["-O3", "-std=c++17", "-lineinfo", "--expt-relaxed-constexpr", "-Xcompi
           "-Xcompiler", "-ffp-contract=off", "-I" + os.path.join(REPO, "include")]
 
 # (source, fmad)
-CUDA_UNITS = [("prep.cu", False), ("disc_plain.cu", False), ("disc_comp.cu", True),
+CUDA_UNITS = [("prep.cu", False), ("disc_plain.cu", False), ("disc_comp.cu", True), ("disc_seg.cu", True),
               ("capi.cu", True), ("noalloc.cu", True), ("adjoint.cu", False),
               ("peaks.cu", True), ("halocore.cu", False)]
 CXX_UNITS = ["frame.cpp"]

@@ -39,7 +39,8 @@ struct dmann_ctx {
     cudaStream_t own = nullptr;
     cudaStream_t stream = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr, evd0 = nullptr, evdm = nullptr, evd1 = nullptr;
-    bool disc_timed = false;
+    cudaEvent_t evp1 = nullptr;   // end of the segmented render's pass 1
+    bool disc_timed = false, seg_timed = false;
     bool have_frame = false, have_units = false;
     double rot[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
     double opos[3] = {0, 0, 0};
@@ -58,6 +59,11 @@ struct dmann_ctx {
     DevBuf cls, oacc, grad;   // the adjoint's class array, observer sums, staged gradient
     DevBuf core_gln;          // the adjoint's d ln(halo-core factor) / d pos, [3][n]
     DevBuf chdr;              // the compensated form's disc headers, one per queue slot
+    // segmented render (disc_seg.cu): work items, per-disc item ranges,
+    // weight sums and pixel counts, and the FP32 deposit plane
+    DevBuf seg_items, seg_first, seg_nit, seg_S, seg_px, plane32;
+    bool seg_plane = false;       // plane32 holds a zeroed plane for the open map
+    long long *h_seg = nullptr;   // pinned: item count, estimated pixels, block-class discs
     // halo cores of the ann_core_nosom law (dmann_set_halo_cores)
     DevBuf halo_f, halo_cells, corr;
     HaloGrid halo{};
@@ -122,6 +128,24 @@ void reserve_headers(dmann_ctx *ctx, size_t n) {
         cudaGetLastError();
         ctx->chdr.p = nullptr;
     }
+}
+
+// An optional buffer: grows like ensure() but a failed allocation is not an
+// error (the caller takes a path that does without it).
+bool ensure_opt(DevBuf &b, size_t bytes) {
+    if (b.bytes >= bytes) return true;
+    if (b.p) cudaFree(b.p);
+    b.p = nullptr;
+    b.bytes = 0;
+    for (size_t want : {bytes + bytes / 8, bytes}) {
+        if (cudaMalloc(&b.p, want) == cudaSuccess) {
+            b.bytes = want;
+            return true;
+        }
+        cudaGetLastError();
+        b.p = nullptr;
+    }
+    return false;
 }
 
 CompHdr *headers_for(const dmann_ctx *ctx, size_t n) {
@@ -243,6 +267,13 @@ dmann_status collect_stats(dmann_ctx *ctx) {
         ctx->stats.disc_block_ms = ms;
         ctx->stats.disc_warp_ms = ctx->stats.disc_ms - ms;
     }
+    ctx->stats.pass1_ms = ctx->stats.pass2_ms = 0.0;
+    if (ctx->seg_timed) {
+        CK(cudaEventElapsedTime(&ms, ctx->evd0, ctx->evp1));
+        ctx->stats.pass1_ms = ms;
+        CK(cudaEventElapsedTime(&ms, ctx->evp1, ctx->evdm));
+        ctx->stats.pass2_ms = ms;
+    }
     ctx->stats.n_kept = ctx->h_ctr[C_KEPT];
     ctx->stats.n_invalid = ctx->h_ctr[C_INVALID];
     ctx->stats.n_single = ctx->h_ctr[C_SINGLE];
@@ -280,8 +311,9 @@ dmann_status dmann_create(dmann_ctx **out, int device) {
         cudaStreamCreateWithFlags(&ctx->own, cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreate(&ctx->ev0) != cudaSuccess || cudaEventCreate(&ctx->ev1) != cudaSuccess ||
         cudaEventCreate(&ctx->evd0) != cudaSuccess || cudaEventCreate(&ctx->evd1) != cudaSuccess ||
-        cudaEventCreate(&ctx->evdm) != cudaSuccess ||
-        cudaHostAlloc((void **)&ctx->h_ctr, 8 * (C_COUNT + 1 + 12), cudaHostAllocDefault) != cudaSuccess) {
+        cudaEventCreate(&ctx->evdm) != cudaSuccess || cudaEventCreate(&ctx->evp1) != cudaSuccess ||
+        cudaHostAlloc((void **)&ctx->h_ctr, 8 * (C_COUNT + 1 + 12), cudaHostAllocDefault) != cudaSuccess ||
+        cudaHostAlloc((void **)&ctx->h_seg, 8 * 4, cudaHostAllocDefault) != cudaSuccess) {
         cudaGetLastError();
         delete ctx;
         return DMANN_ERR_CUDA;
@@ -306,7 +338,8 @@ void dmann_destroy(dmann_ctx *ctx) {
                       &ctx->theta, &ctx->phi, &ctx->ar, &ctx->flux, &ctx->cpix, &ctx->key,
                       &ctx->queue, &ctx->hist, &ctx->ctr, &ctx->fsum, &ctx->acc, &ctx->map,
                       &ctx->cls, &ctx->oacc, &ctx->grad, &ctx->halo_f, &ctx->halo_cells,
-                      &ctx->corr, &ctx->chdr, &ctx->core_gln};
+                      &ctx->corr, &ctx->chdr, &ctx->core_gln, &ctx->seg_items, &ctx->seg_first,
+                      &ctx->seg_nit, &ctx->seg_S, &ctx->seg_px, &ctx->plane32};
     for (DevBuf *b : bufs)
         if (b->p) cudaFree(b->p);
     for (auto &kv : ctx->rings) {
@@ -318,10 +351,12 @@ void dmann_destroy(dmann_ctx *ctx) {
         cudaFree(kv.second.step32);
     }
     if (ctx->h_ctr) cudaFreeHost(ctx->h_ctr);
+    if (ctx->h_seg) cudaFreeHost(ctx->h_seg);
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
     if (ctx->evd0) cudaEventDestroy(ctx->evd0);
     if (ctx->evd1) cudaEventDestroy(ctx->evd1);
     if (ctx->evdm) cudaEventDestroy(ctx->evdm);
+    if (ctx->evp1) cudaEventDestroy(ctx->evp1);
     if (ctx->ev1) cudaEventDestroy(ctx->ev1);
     if (ctx->own) cudaStreamDestroy(ctx->own);
     delete ctx;
@@ -583,6 +618,62 @@ Accum make_accum(dmann_ctx *ctx) {
     return acc;
 }
 
+// The compensated form's block-class discs in work items and segments
+// (disc_seg.cu), then the warp class with the per-disc kernel.  Needs the
+// disc headers, the FP32 plane and the item buffers; without any of them
+// `used` stays false and the caller renders with the per-disc kernels.
+// Reads the item count back to the host (one synchronisation per chunk) to
+// size the item list and the segment count.
+dmann_status render_segmented(dmann_ctx *ctx, const DiscArgs &da, const dmann_tuning &tu, size_t N,
+                              bool &used) {
+    used = false;
+    if (!da.chdr || !ctx->seg_plane) return DMANN_OK;
+    const size_t n1 = N > 0 ? N : 1;
+    if (!ensure_opt(ctx->seg_first, 8 * n1) || !ensure_opt(ctx->seg_nit, 4 * n1) ||
+        !ensure_opt(ctx->seg_S, 8 * n1) || !ensure_opt(ctx->seg_px, 8 * n1))
+        return DMANN_OK;
+    cudaStream_t s = ctx->stream;
+    const int bt = tu.block_threads == 256 ? 256 : 128;
+    SegArgs sg{};
+    sg.disc_first = (long long *)ctx->seg_first.p;
+    sg.disc_nitems = (int *)ctx->seg_nit.p;
+    sg.disc_S = (double *)ctx->seg_S.p;
+    sg.disc_px = (long long *)ctx->seg_px.p;
+    sg.plane = (float *)ctx->plane32.p;
+    CK(launch_hdr(da, ctx->num_sms, s));
+    CK(launch_seg_count(da, sg, bt, ctx->num_sms, s));
+    CK(cudaMemcpyAsync(ctx->h_seg, (long long *)ctx->ctr.p + C_SEG_ITEMS, 16, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(ctx->h_seg + 2, (long long *)ctx->ctr.p + C_ADD_BLOCK, 8, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    const long long items = ctx->h_seg[0], est = ctx->h_seg[1], nblk = ctx->h_seg[2];
+    if (items > 0 && !ensure_opt(ctx->seg_items, 8 * (size_t)items)) {
+        // no room for the item list: the per-disc kernels take the chunk
+        CK(launch_disc_comp(da, ctx->num_sms, tu.blocks_per_sm, tu.block_threads, s, ctx->evdm));
+        ctx->launches += 8;   // prep, scan, scatter, headers, item count, headers, block, warp
+        used = true;
+        return DMANN_OK;
+    }
+    sg.items = (int2 *)ctx->seg_items.p;
+    sg.n_items = items;
+    const double per_pix = (double)est / (double)ctx->g.npix;
+    sg.n_seg = (int)std::min<double>(kSegMax, std::max(1.0, std::ceil(per_pix / kDepPerPix)));
+    if (nblk > 0) {
+        CK(cudaMemsetAsync(sg.disc_S, 0, 8 * (size_t)nblk, s));
+        CK(cudaMemsetAsync(sg.disc_px, 0, 8 * (size_t)nblk, s));
+    }
+    CK(launch_seg_norm(da, sg, bt, ctx->num_sms, tu.blocks_per_sm, s));
+    CK(cudaEventRecord(ctx->evp1, s));
+    CK(launch_seg_deposits(da, sg, bt, ctx->num_sms, tu.blocks_per_sm, ctx->g.npix, s));
+    CK(cudaEventRecord(ctx->evdm, s));
+    CK(launch_disc_comp_warp(da, ctx->num_sms, s));
+    ctx->seg_timed = true;
+    // prep, scan, scatter, headers, item count, item fill, pass 1, K x (deposits,
+    // flush), warp class
+    ctx->launches += 8 + 2 * sg.n_seg;
+    used = true;
+    return DMANN_OK;
+}
+
 }  // namespace
 
 // Every context call that uses the accumulation planes, the queue or the
@@ -614,9 +705,14 @@ dmann_status dmann_map_begin(dmann_ctx *ctx, int nside, int precision) {
     CK(cudaMemsetAsync(ctx->acc.p, 0, 8 * P, s));
     CK(cudaMemsetAsync(ctx->ctr.p, 0, 8 * C_COUNT, s));
     CK(cudaMemsetAsync(ctx->fsum.p, 0, 8, s));
+    // the segmented render's FP32 plane: zero at the start of a map, and
+    // every segment's flush leaves it zero
+    ctx->seg_plane = precision == DMANN_COMP_F32 && ensure_opt(ctx->plane32, 4 * P);
+    if (ctx->seg_plane) CK(cudaMemsetAsync(ctx->plane32.p, 0, 4 * P, s));
     ctx->stats = dmann_stats{};
     ctx->launches = 0;
     ctx->disc_timed = false;
+    ctx->seg_timed = false;
     ctx->in_map = true;
     return DMANN_OK;
 }
@@ -706,11 +802,18 @@ dmann_status dmann_map_add_v(dmann_ctx *ctx, const float *x, const float *y, con
     da.acc = acc;
     if (ctx->precision == DMANN_COMP_F32) da.chdr = headers_for(ctx, N);
     CK(cudaEventRecord(ctx->evd0, s));
-    if (ctx->precision == DMANN_PLAIN_F64) CK(launch_disc_plain(da, ctx->num_sms, tu.blocks_per_sm, s, ctx->evdm));
-    else CK(launch_disc_comp(da, ctx->num_sms, tu.blocks_per_sm, tu.block_threads, s, ctx->evdm));
+    if (ctx->precision == DMANN_PLAIN_F64) {
+        CK(launch_disc_plain(da, ctx->num_sms, tu.blocks_per_sm, s, ctx->evdm));
+        ctx->launches += 5;   // prep, scan, scatter, disc block, disc warp
+    } else {
+        bool seg = false;
+        if ((st = render_segmented(ctx, da, tu, N, seg)) != DMANN_OK) return st;
+        if (!seg) {
+            CK(launch_disc_comp(da, ctx->num_sms, tu.blocks_per_sm, tu.block_threads, s, ctx->evdm));
+            ctx->launches += 5 + (da.chdr ? 1 : 0);   // prep, scan, scatter, headers, block, warp
+        }
+    }
     CK(cudaEventRecord(ctx->evd1, s));
-    // prep, scan, scatter, the disc kernels (block, warp; headers when held)
-    ctx->launches += 5 + (da.chdr ? 1 : 0);
     ctx->disc_timed = true;
     return DMANN_OK;
 }

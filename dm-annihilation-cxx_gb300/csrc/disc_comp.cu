@@ -352,13 +352,22 @@ __global__ void __launch_bounds__(256) k_comp_hdr(DiscArgs a) {
     }
 }
 
+}  // namespace
+
 cudaError_t launch_hdr(const DiscArgs &a, int num_sms, cudaStream_t s) {
     if (!a.chdr) return cudaSuccess;
     k_comp_hdr<<<num_sms * 8, 256, 0, s>>>(a);
     return cudaGetLastError();
 }
 
-}  // namespace
+cudaError_t launch_disc_comp_warp(const DiscArgs &a, int num_sms, cudaStream_t s) {
+    int occw = 0;
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occw, k_comp_warp, kWPB * 32, 0);
+    if (e != cudaSuccess) return e;
+    if (occw < 1) occw = 1;
+    k_comp_warp<<<num_sms * occw, kWPB * 32, 0, s>>>(a);
+    return cudaGetLastError();
+}
 
 size_t comp_hdr_bytes() { return sizeof(CompHdr); }
 

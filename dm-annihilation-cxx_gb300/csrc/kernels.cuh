@@ -21,9 +21,19 @@ constexpr int kKeys = kBuckets * kCells;
 // Device counters (int64).  The first six accumulate over every chunk of
 // a map; the C_ADD_* ones describe the chunk being added and are reset for
 // each chunk.
+// Segmented render (disc_seg.cu): at most kSegMax segments of the FP32
+// plane per chunk, each taking about kDepPerPix FP32 additions per pixel.
+constexpr int kSegMax = 32;
+constexpr int kDepPerPix = 512;
+
 enum Ctr {
     C_KEPT = 0, C_SINGLE, C_DISC, C_DISC_BLOCK, C_DEPOSITS, C_INVALID,
-    C_ADD_DISC, C_ADD_BLOCK, C_QNEXT_BLOCK, C_QNEXT_WARP, C_COUNT
+    C_ADD_DISC, C_ADD_BLOCK, C_QNEXT_BLOCK, C_QNEXT_WARP,
+    C_SEG_ITEMS,       // work items of the chunk's block-class discs
+    C_SEG_EST,         // their estimated pixels (cap areas)
+    C_SEG_NEXT_NORM,   // items claimed by pass 1
+    C_SEG_NEXT_DEP,    // kSegMax counters: items claimed by each segment
+    C_COUNT = C_SEG_NEXT_DEP + kSegMax
 };
 constexpr int kCtrChunkFirst = C_ADD_DISC;
 
@@ -91,6 +101,18 @@ struct DiscArgs {
     CompHdr *chdr = nullptr;
 };
 
+// Segmented render of the block-class discs (disc_seg.cu).
+struct SegArgs {
+    int2 *items;              // (queue slot, item index within its disc)
+    long long n_items;
+    long long *disc_first;    // per block-class disc: its first item
+    int *disc_nitems;         //   its item count
+    double *disc_S;           //   the sum of its weights (pass 1; zeroed by the caller)
+    long long *disc_px;       //   its pixel count (pass 1; zeroed by the caller)
+    float *plane;             // FP32 deposit plane, npix floats, zero between segments
+    int n_seg;                // segments K (1 .. kSegMax)
+};
+
 // prep.cu
 cudaError_t launch_prep(const PrepArgs &a, cudaStream_t s);
 cudaError_t launch_scan(int *hist, long long *ctr, int block_bucket_min, cudaStream_t s);
@@ -111,6 +133,19 @@ cudaError_t launch_disc_plain(const DiscArgs &a, int num_sms, int blocks_per_sm,
 cudaError_t launch_disc_comp(const DiscArgs &a, int num_sms, int blocks_per_sm, int block_threads,
                              cudaStream_t s, cudaEvent_t mid);
 size_t comp_hdr_bytes();
+// the headers of every queued disc (k_comp_hdr; nothing when a.chdr is null)
+cudaError_t launch_hdr(const DiscArgs &a, int num_sms, cudaStream_t s);
+// the warp-per-particle compensated kernel alone (the warp class)
+cudaError_t launch_disc_comp_warp(const DiscArgs &a, int num_sms, cudaStream_t s);
+// disc_seg.cu: the item count of every block-class disc (needs the headers);
+// the item list and pass 1; the n_seg segments of deposits, each followed by
+// its flush.  block_threads 128 or 256 picks the block shape.
+cudaError_t launch_seg_count(const DiscArgs &a, const SegArgs &sg, int block_threads, int num_sms,
+                             cudaStream_t s);
+cudaError_t launch_seg_norm(const DiscArgs &a, const SegArgs &sg, int block_threads, int num_sms,
+                            int blocks_per_sm, cudaStream_t s);
+cudaError_t launch_seg_deposits(const DiscArgs &a, const SegArgs &sg, int block_threads, int num_sms,
+                                int blocks_per_sm, int npix, cudaStream_t s);
 // adjoint.cu: gradients of the plain-form map for dL/dmap = gmap; grad is
 // [6][n] (x, y, z, m, rho, h); oacc[12] (zeroed by the caller) receives
 // sum_i dL/du_i and dL/drot (row-major).  Needs the prep outputs (with cls)

@@ -34,7 +34,8 @@ class Stats(C.Structure):
                 ("n_disc", C.c_int64), ("n_disc_block", C.c_int64), ("deposits", C.c_int64),
                 ("kernel_ms", C.c_double), ("disc_ms", C.c_double),
                 ("disc_block_ms", C.c_double), ("disc_warp_ms", C.c_double),
-                ("total_flux", C.c_double), ("launches", C.c_int64)]
+                ("total_flux", C.c_double), ("launches", C.c_int64),
+                ("pass1_ms", C.c_double), ("pass2_ms", C.c_double)]
 
 
 class Tuning(C.Structure):

@@ -105,6 +105,10 @@ typedef struct {
     double disc_warp_ms;   /* of which the warp-per-particle kernel */
     double total_flux;     /* sum of kept flux (before the dOmega division) */
     int64_t launches;      /* kernels launched for the last map (all chunks) */
+    double pass1_ms;       /* compensated form, block class of the last chunk: from the
+                              disc kernels' start to the end of the weight sums (headers,
+                              work items, pass 1) */
+    double pass2_ms;       /* the deposit segments and their flushes */
 } dmann_stats;
 
 /* Tunables (set by the annmap autotuner; zero fields keep the current
