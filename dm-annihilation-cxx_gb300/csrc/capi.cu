@@ -61,7 +61,7 @@ struct dmann_ctx {
     DevBuf chdr;              // the compensated form's disc headers, one per queue slot
     // segmented render (disc_seg.cu): work items, per-disc item ranges,
     // weight sums and pixel counts, and the FP32 deposit plane
-    DevBuf seg_items, seg_first, seg_nit, seg_S, seg_px, plane32;
+    DevBuf seg_items, seg_sorted, seg_cls, seg_first, seg_nit, seg_S, seg_px, plane32;
     bool seg_plane = false;       // plane32 holds a zeroed plane for the open map
     long long *h_seg = nullptr;   // pinned: item count, estimated pixels, block-class discs
     // halo cores of the ann_core_nosom law (dmann_set_halo_cores)
@@ -338,7 +338,8 @@ void dmann_destroy(dmann_ctx *ctx) {
                       &ctx->theta, &ctx->phi, &ctx->ar, &ctx->flux, &ctx->cpix, &ctx->key,
                       &ctx->queue, &ctx->hist, &ctx->ctr, &ctx->fsum, &ctx->acc, &ctx->map,
                       &ctx->cls, &ctx->oacc, &ctx->grad, &ctx->halo_f, &ctx->halo_cells,
-                      &ctx->corr, &ctx->chdr, &ctx->core_gln, &ctx->seg_items, &ctx->seg_first,
+                      &ctx->corr, &ctx->chdr, &ctx->core_gln, &ctx->seg_items, &ctx->seg_sorted,
+                      &ctx->seg_cls, &ctx->seg_first,
                       &ctx->seg_nit, &ctx->seg_S, &ctx->seg_px, &ctx->plane32};
     for (DevBuf *b : bufs)
         if (b->p) cudaFree(b->p);
@@ -630,7 +631,8 @@ dmann_status render_segmented(dmann_ctx *ctx, const DiscArgs &da, const dmann_tu
     if (!da.chdr || !ctx->seg_plane) return DMANN_OK;
     const size_t n1 = N > 0 ? N : 1;
     if (!ensure_opt(ctx->seg_first, 8 * n1) || !ensure_opt(ctx->seg_nit, 4 * n1) ||
-        !ensure_opt(ctx->seg_S, 8 * n1) || !ensure_opt(ctx->seg_px, 8 * n1))
+        !ensure_opt(ctx->seg_S, 8 * n1) || !ensure_opt(ctx->seg_px, 8 * n1) ||
+        !ensure_opt(ctx->seg_cls, 4 * 512))
         return DMANN_OK;
     cudaStream_t s = ctx->stream;
     const int bt = tu.block_threads == 256 ? 256 : 128;
@@ -646,7 +648,8 @@ dmann_status render_segmented(dmann_ctx *ctx, const DiscArgs &da, const dmann_tu
     CK(cudaMemcpyAsync(ctx->h_seg + 2, (long long *)ctx->ctr.p + C_ADD_BLOCK, 8, cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
     const long long items = ctx->h_seg[0], est = ctx->h_seg[1], nblk = ctx->h_seg[2];
-    if (items > 0 && !ensure_opt(ctx->seg_items, 8 * (size_t)items)) {
+    if (items > 0 && (!ensure_opt(ctx->seg_items, 8 * (size_t)items) ||
+                      !ensure_opt(ctx->seg_sorted, 8 * (size_t)items))) {
         // no room for the item list: the per-disc kernels take the chunk
         CK(launch_disc_comp(da, ctx->num_sms, tu.blocks_per_sm, tu.block_threads, s, ctx->evdm));
         ctx->launches += 8;   // prep, scan, scatter, headers, item count, headers, block, warp
@@ -654,6 +657,8 @@ dmann_status render_segmented(dmann_ctx *ctx, const DiscArgs &da, const dmann_tu
         return DMANN_OK;
     }
     sg.items = (int2 *)ctx->seg_items.p;
+    sg.sorted = (int2 *)ctx->seg_sorted.p;
+    sg.cls = (int *)ctx->seg_cls.p;
     sg.n_items = items;
     const double per_pix = (double)est / (double)ctx->g.npix;
     sg.n_seg = (int)std::min<double>(kSegMax, std::max(1.0, std::ceil(per_pix / kDepPerPix)));
@@ -661,15 +666,16 @@ dmann_status render_segmented(dmann_ctx *ctx, const DiscArgs &da, const dmann_tu
         CK(cudaMemsetAsync(sg.disc_S, 0, 8 * (size_t)nblk, s));
         CK(cudaMemsetAsync(sg.disc_px, 0, 8 * (size_t)nblk, s));
     }
+    CK(cudaMemsetAsync(sg.cls, 0, 4 * 512, s));
     CK(launch_seg_norm(da, sg, bt, ctx->num_sms, tu.blocks_per_sm, s));
     CK(cudaEventRecord(ctx->evp1, s));
     CK(launch_seg_deposits(da, sg, bt, ctx->num_sms, tu.blocks_per_sm, ctx->g.npix, s));
     CK(cudaEventRecord(ctx->evdm, s));
     CK(launch_disc_comp_warp(da, ctx->num_sms, s));
     ctx->seg_timed = true;
-    // prep, scan, scatter, headers, item count, item fill, pass 1, K x (deposits,
-    // flush), warp class
-    ctx->launches += 8 + 2 * sg.n_seg;
+    // prep, scan, scatter, headers, item count, item fill, pass 1, item sort
+    // (3), K x (deposits, flush), warp class
+    ctx->launches += 11 + 2 * sg.n_seg;
     used = true;
     return DMANN_OK;
 }

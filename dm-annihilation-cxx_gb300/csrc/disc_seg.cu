@@ -39,11 +39,21 @@
 //
 // Deposits and segments.  A deposit w (F + Flo) is rounded once to FP32 and
 // added with red.global.add.f32 into an FP32 plane: half the L2 reduction
-// bytes of an FP64 deposit.  To bound the error of those FP32 sums the items
-// are dealt into K segments (item k to segment k mod K, so each segment is a
-// uniform sample of all discs); after each segment k_seg_flush adds the FP32
-// plane into the FP64 plane and clears it.  K is chosen so that a pixel
-// takes about kDepPerPix FP32 additions per segment.
+// bytes of an FP64 deposit.  Two things keep those FP32 sums accurate.
+//   * Order.  The particles' deposit scales F span many decades, and a
+//     round-to-nearest FP32 sum drops any addend below half an ulp of the
+//     running total: small deposits arriving after large ones would be lost
+//     (a bias, always downwards).  After pass 1 the items are therefore
+//     sorted by the octave of F (a counting sort, k_seg_class .. k_seg_sort)
+//     and deposited in ascending order: a pixel's running total is then made
+//     of deposits no larger than the next one's disc scale, every addend
+//     stays many ulps above the total's rounding, and the rounding errors
+//     are unbiased.
+//   * Length.  The sorted items are dealt into K segments (item k to segment
+//     k mod K: each segment is an ascending sample of all discs); after each
+//     segment k_seg_flush adds the FP32 plane into the FP64 plane and clears
+//     it.  K is chosen so that a pixel takes about kDepPerPix FP32 additions
+//     per segment.
 #include "comp_engine.cuh"
 
 namespace dmann {
@@ -51,6 +61,7 @@ namespace dmann {
 namespace {
 
 constexpr int kItemPx = 32768;   // pixels per work item (from the disc's cap-area estimate)
+constexpr int kClasses = 256;    // octaves of the deposit scale F (the item sort's keys)
 
 // One staged run: a ring's pixels inside the disc, contiguous in the map.
 struct alignas(16) SRun {
@@ -188,9 +199,9 @@ __device__ inline void seg_walk(SegSmem<RCH> &sm, int n, Body body, Done ring_do
 // the t-th claim) and stages its disc's header; false when the item range
 // is exhausted.
 template <int BT, int RCH>
-__device__ inline bool seg_claim(const DiscArgs &a, const SegArgs &sg, SegSmem<RCH> &sm,
-                                 unsigned long long *next, long long stride, long long first,
-                                 int2 &it) {
+__device__ inline bool seg_claim(const DiscArgs &a, const SegArgs &sg, const int2 *items,
+                                 SegSmem<RCH> &sm, unsigned long long *next, long long stride,
+                                 long long first, int2 &it) {
     if (threadIdx.x == 0) {
         const long long t = (long long)atomicAdd(next, 1ull);
         const long long k = first + t * stride;
@@ -199,7 +210,7 @@ __device__ inline bool seg_claim(const DiscArgs &a, const SegArgs &sg, SegSmem<R
     __syncthreads();
     const int k = sm.item;
     if (k < 0) return false;
-    it = sg.items[k];
+    it = items[k];
     constexpr int kWords = sizeof(CompHdr) / 8;
     static_assert(kWords <= BT, "one header word per thread");
     if (threadIdx.x < kWords)
@@ -254,7 +265,8 @@ template <int BT, int RCH, int MINB>
 __global__ void __launch_bounds__(BT, MINB) k_seg_norm(DiscArgs a, SegArgs sg) {
     __shared__ SegSmem<RCH> sm;
     int2 it;
-    while (seg_claim<BT, RCH>(a, sg, sm, (unsigned long long *)(a.ctr + C_SEG_NEXT_NORM), 1, 0, it)) {
+    while (seg_claim<BT, RCH>(a, sg, sg.items, sm, (unsigned long long *)(a.ctr + C_SEG_NEXT_NORM), 1, 0,
+                              it)) {
         int r0, n;
         item_rings(sm.h, it.y, r0, n);
         const bool poly = sm.h.ext.tier_x < 2 && sm.h.ext.tier_h < 2;
@@ -290,12 +302,12 @@ __device__ inline void dep_item(const DiscArgs &a, SegSmem<RCH> &sm, int r0, int
     __syncthreads();
 }
 
-// Segment s: items s, s + K, s + 2K, ...
+// Segment s: items s, s + K, s + 2K, ... of the sorted list (ascending F).
 template <int BT, int RCH, int MINB>
 __global__ void __launch_bounds__(BT, MINB) k_seg_dep(DiscArgs a, SegArgs sg, int s) {
     __shared__ SegSmem<RCH> sm;
     int2 it;
-    while (seg_claim<BT, RCH>(a, sg, sm, (unsigned long long *)(a.ctr + C_SEG_NEXT_DEP + s),
+    while (seg_claim<BT, RCH>(a, sg, sg.sorted, sm, (unsigned long long *)(a.ctr + C_SEG_NEXT_DEP + s),
                               sg.n_seg, s, it)) {
         const long long total = sg.disc_px[it.x];
         const double fs = sm.h.hdr.flux * a.f.inv_scale;
@@ -360,6 +372,56 @@ __global__ void __launch_bounds__(256) k_seg_fill(DiscArgs a, SegArgs sg) {
     }
 }
 
+// The item sort's key of block-class disc q: the octave of its deposit
+// scale F = flux * inv_scale / S (class 0 for discs that deposit no
+// weighted pixels: fewer than two pixels, or zero flux).
+__device__ inline int seg_class(const DiscArgs &a, const SegArgs &sg, long long q) {
+    const double S = sg.disc_S[q];
+    const double F = a.chdr[q].hdr.flux * a.f.inv_scale / S;
+    if (sg.disc_px[q] < 2 || !(F > 0.0) || !isfinite(F)) return 0;
+    return min(kClasses - 1, max(1, ilogb(F) + kClasses / 2));
+}
+
+// Items per class (the histogram, sg.cls[0 .. kClasses)).
+__global__ void __launch_bounds__(256) k_seg_class(DiscArgs a, SegArgs sg) {
+    __shared__ int hist[kClasses];
+    for (int i = threadIdx.x; i < kClasses; i += blockDim.x) hist[i] = 0;
+    __syncthreads();
+    const long long nblk = a.ctr[C_ADD_BLOCK];
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < nblk; q += stride)
+        atomicAdd(&hist[seg_class(a, sg, q)], sg.disc_nitems[q]);
+    __syncthreads();
+    for (int i = threadIdx.x; i < kClasses; i += blockDim.x)
+        if (hist[i]) atomicAdd(sg.cls + i, hist[i]);
+}
+
+// Exclusive scan of the class histogram into the classes' first slots
+// (sg.cls[kClasses .. 2 kClasses)); one block of kClasses threads.
+__global__ void __launch_bounds__(kClasses) k_seg_cscan(SegArgs sg) {
+    int total;
+    const int v = sg.cls[threadIdx.x];
+    const int ex = warp_excl_scan(v, total);
+    __shared__ int wsum[kClasses / 32];
+    if ((threadIdx.x & 31) == 0) wsum[threadIdx.x >> 5] = total;
+    __syncthreads();
+    int base = 0;
+    for (int w = 0; w < (int)(threadIdx.x >> 5); w++) base += wsum[w];
+    sg.cls[kClasses + threadIdx.x] = base + ex;
+}
+
+// Each disc's items into its class's range of the sorted list.
+__global__ void __launch_bounds__(256) k_seg_sort(DiscArgs a, SegArgs sg) {
+    const long long nblk = a.ctr[C_ADD_BLOCK];
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < nblk; q += stride) {
+        const int nit = sg.disc_nitems[q];
+        const long long f = atomicAdd(sg.cls + kClasses + seg_class(a, sg, q), nit);
+        for (int i = 0; i < nit; i++)
+            if (f + i < sg.n_items) sg.sorted[f + i] = make_int2((int)q, i);
+    }
+}
+
 // acc64 += plane, plane = 0 (four pixels per thread; npix is a multiple of 4).
 __global__ void __launch_bounds__(256) k_seg_flush(float *plane, double *acc, long long npix4) {
     const long long stride = (long long)gridDim.x * blockDim.x;
@@ -399,11 +461,23 @@ cudaError_t launch_norm(const DiscArgs &a, const SegArgs &sg, int num_sms, int b
     return cudaGetLastError();
 }
 
+// The item list sorted by the octave of each disc's deposit scale.
+cudaError_t launch_sort(const DiscArgs &a, const SegArgs &sg, int num_sms, cudaStream_t s) {
+    k_seg_class<<<num_sms * 4, 256, 0, s>>>(a, sg);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    k_seg_cscan<<<1, kClasses, 0, s>>>(sg);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    k_seg_sort<<<num_sms * 8, 256, 0, s>>>(a, sg);
+    return cudaGetLastError();
+}
+
 template <int BT, int RCH, int MINB>
 cudaError_t launch_deposits(const DiscArgs &a, const SegArgs &sg, int num_sms, int blocks_per_sm, int npix,
                             cudaStream_t s) {
     const int grid = grid_of<BT, RCH, MINB>(num_sms, blocks_per_sm);
-    cudaError_t e;
+    cudaError_t e = launch_sort(a, sg, num_sms, s);
+    if (e != cudaSuccess) return e;
     for (int seg = 0; seg < sg.n_seg; seg++) {
         k_seg_dep<BT, RCH, MINB><<<grid, BT, 0, s>>>(a, sg, seg);
         if ((e = cudaGetLastError()) != cudaSuccess) return e;

@@ -103,7 +103,9 @@ struct DiscArgs {
 
 // Segmented render of the block-class discs (disc_seg.cu).
 struct SegArgs {
-    int2 *items;              // (queue slot, item index within its disc)
+    int2 *items;              // (queue slot, item index within its disc), queue order
+    int2 *sorted;             // the same items in ascending octave of the disc's F
+    int *cls;                 // [2 x 256]: items per octave, then each octave's first slot
     long long n_items;
     long long *disc_first;    // per block-class disc: its first item
     int *disc_nitems;         //   its item count
