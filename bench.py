@@ -149,8 +149,8 @@ def measured_peaks():
 
 
 def profile_traffic():
-    """Per-launch DRAM bytes of the disc kernels from the committed ncu summary."""
-    p = os.path.join(REPO, "profiles", "disc_comp_traffic.json")
+    """Per-deposit DRAM bytes of the deposit kernel from the committed ncu summary."""
+    p = os.path.join(REPO, "profiles", "disc_seg_traffic.json")
     if os.path.exists(p):
         with open(p) as f:
             return json.load(f)
@@ -159,17 +159,54 @@ def profile_traffic():
 
 def measure_l2_red(device, nbytes=400_000_000):
     """Live L2 reduction rates (operations/s) of the library's own sweep
-    microbenchmark over a 400 MB array: FP64 red (the deposit of both forms),
-    FP32 red and the returning-atomic compensated FP32 deposit."""
+    microbenchmark over a 400 MB array: FP32 red (the compensated form's
+    deposit) and FP64 red (the plain form's)."""
     import ctypes as C
     from annmap import _lib
     L = _lib.load()
     out = {}
-    for name, kind, reps in (("red_f32", 0, 20), ("comp_f32", 2, 10), ("red_f64", 1, 20)):
+    for name, kind, reps in (("red_f32", 0, 20), ("red_f64", 1, 20)):
         v = C.c_double()
         st = L.dmann_measure_l2_red(int(device), kind, int(nbytes), reps, C.byref(v))
         out[name] = v.value if st == 0 else None
     return out
+
+
+FP32_FLOPS_PER_WEIGHT = 12   # x (FMA), y = x^2, 4 Horner FMAs, the sum: 2 + 1 + 8 + 1
+
+
+def roofline(device, deposits, pass1_ms, pass2_ms):
+    """The deposit pass's roofline on its binding resource, the L2 reduction
+    units: each algorithmic deposit is one FP32 reduction (4 B) into the
+    map's FP32 plane, against the library's live red.global.add.f32 sweep.
+    Beside it the same bytes against measured HBM, and pass 1 (weight sums:
+    FP32 arithmetic, no memory traffic to speak of) against the nominal FP32
+    rate of the FMA pipes."""
+    l2 = measure_l2_red(device)
+    hbm, hbm_src = measured_peaks()
+    red_bytes = 4.0 * deposits
+    s2, s1 = pass2_ms / 1e3, pass1_ms / 1e3
+    achieved = red_bytes / s2 / 1e9
+    peak = (l2["red_f32"] or 0.0) * 4.0 / 1e9
+    traffic = profile_traffic()
+    nominal_fp32 = 152 * 128 * 2 * 2.07e9 / 1e12
+    p1_tflops = deposits * FP32_FLOPS_PER_WEIGHT / s1 / 1e12
+    return {"bound": "l2_red", "kernel": "k_seg_dep (deposit segments)", "achieved": achieved,
+            "peak": peak, "unit": "GB/s", "frac": achieved / peak if peak else None,
+            "peak_source": (f"measured here: red.global.add.f32 sweep over 400 MB "
+                            f"({l2['red_f32']:.3e} reductions/s)") if l2["red_f32"] else "unavailable",
+            "traffic": (traffic["dram_bytes_per_deposit"] * deposits) if traffic else None,
+            "traffic_source": traffic.get("capture") if traffic else None,
+            "algorithmic_bytes": red_bytes,
+            "basis": "4 B FP32 reduction per algorithmic deposit / deposit-pass time (CUDA events)",
+            "hbm": {"achieved": achieved, "peak": hbm, "frac": achieved / hbm,
+                    "peak_source": hbm_src + " (MEASURED_PEAKS hbm_gbs)"},
+            "red_f64_sweep_ops": l2["red_f64"],
+            "pass1": {"kernel": "k_seg_norm (weight sums)", "ms": pass1_ms, "weights_per_s": deposits / s1,
+                      "fp32_flops_per_weight": FP32_FLOPS_PER_WEIGHT, "achieved_tflops": p1_tflops,
+                      "peak_tflops": nominal_fp32,
+                      "peak_source": "nominal: 152 SMs x 128 FP32 lanes x FMA x 2.07 GHz",
+                      "frac": p1_tflops / nominal_fp32}}
 
 
 def rel_err(got, ref):
@@ -311,11 +348,14 @@ def run_gb300(args, ws, rank, local):
         torch.cuda.synchronize()
         e0.record(stream)
         launches = 0
+        p1_ms, p2_ms = [], []
         for _ in range(args.steps):
             r.render(dparts, nside, annmap.COMP_F32, out=dmap)
             step_stats = r.stats()
             disc_ms.append(step_stats["disc_ms"])
             step_ms.append(step_stats["kernel_ms"])
+            p1_ms.append(step_stats["pass1_ms"])
+            p2_ms.append(step_stats["pass2_ms"])
             launches += step_stats["launches"]
         e1.record(stream)
         torch.cuda.synchronize()
@@ -344,32 +384,9 @@ def run_gb300(args, ws, rank, local):
                          "disc_block": step_stats["disc_block_ms"], "disc_warp": step_stats["disc_warp_ms"],
                          "per_step": [round(x, 2) for x in step_ms]}}
 
-    # roofline of the dominant kernels (the disc kernels): one 8-byte
-    # read-modify-write reduction per algorithmic deposit
-    peak, peak_src = measured_peaks()
-    dms = statistics.mean(disc_ms)
-    alg_bytes = 8.0 * step_stats["deposits"]
-    achieved = alg_bytes / (dms / 1e3) / 1e9
-    traffic = profile_traffic()
-    line["roofline"] = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                        "frac": achieved / peak, "peak_source": peak_src,
-                        # the captured launch's DRAM bytes per deposit (ncu, 2M-particle
-                        # prefix) times this launch's deposits
-                        "traffic": traffic["dram_bytes_per_deposit"] * step_stats["deposits"] if traffic else None,
-                        "algorithmic_bytes": alg_bytes,
-                        "basis": "8 B per deposit (FP64 map read-modify-write) / disc-kernel time"}
-    # the deposit scatter against the L2 reduction rates measured here
-    l2 = measure_l2_red(local)
-    dep_rate = step_stats["deposits"] / (dms / 1e3)
-    line["roofline"]["l2_red"] = {
-        "achieved_ops": dep_rate, "unit": "reductions/s",
-        "peak_red_f32_ops": l2["red_f32"], "peak_comp_f32_ops": l2["comp_f32"],
-        "peak_red_f64_ops": l2["red_f64"],
-        # each deposit is one red.global.add.f64
-        "frac_red_f64": dep_rate / l2["red_f64"] if l2["red_f64"] else None,
-        "frac_red_f32": dep_rate / l2["red_f32"] if l2["red_f32"] else None,
-        "frac_comp_f32": dep_rate / l2["comp_f32"] if l2["comp_f32"] else None,
-        "basis": "deposits / disc-kernel time vs a coalesced sweep of reductions over 400 MB"}
+    line["stage_ms"].update({"pass1": statistics.mean(p1_ms), "pass2": statistics.mean(p2_ms)})
+    line["roofline"] = roofline(local, step_stats["deposits"], statistics.mean(p1_ms),
+                                statistics.mean(p2_ms))
 
     if not args.no_extras and rank == 0:
         # plain FP64 form on a prefix (the plain form is FP64-throughput bound)
