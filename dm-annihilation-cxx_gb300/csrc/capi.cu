@@ -63,7 +63,9 @@ struct dmann_ctx {
     // weight sums and pixel counts, and the FP32 deposit plane
     DevBuf seg_items, seg_sorted, seg_cls, seg_first, seg_nit, seg_S, seg_px, plane32;
     bool seg_plane = false;       // plane32 holds a zeroed plane for the open map
-    long long *h_seg = nullptr;   // pinned: item count, estimated pixels, block-class discs
+    // pinned: item count, estimated pixels, block-class discs (4 slots), then
+    // the per-octave item counts, first slots and pixels (the segment plan)
+    long long *h_seg = nullptr;
     // halo cores of the ann_core_nosom law (dmann_set_halo_cores)
     DevBuf halo_f, halo_cells, corr;
     HaloGrid halo{};
@@ -313,7 +315,8 @@ dmann_status dmann_create(dmann_ctx **out, int device) {
         cudaEventCreate(&ctx->evd0) != cudaSuccess || cudaEventCreate(&ctx->evd1) != cudaSuccess ||
         cudaEventCreate(&ctx->evdm) != cudaSuccess || cudaEventCreate(&ctx->evp1) != cudaSuccess ||
         cudaHostAlloc((void **)&ctx->h_ctr, 8 * (C_COUNT + 1 + 12), cudaHostAllocDefault) != cudaSuccess ||
-        cudaHostAlloc((void **)&ctx->h_seg, 8 * 4, cudaHostAllocDefault) != cudaSuccess) {
+        cudaHostAlloc((void **)&ctx->h_seg, 8 * 4 + kSegClsBytes + kSegClsPxBytes, cudaHostAllocDefault) !=
+            cudaSuccess) {
         cudaGetLastError();
         delete ctx;
         return DMANN_ERR_CUDA;
@@ -325,6 +328,7 @@ dmann_status dmann_create(dmann_ctx **out, int device) {
     ctx->tune.block_threads = 256;
     ctx->tune.blocks_per_sm = 0;
     ctx->tune.ring_chunk = 384;
+    ctx->tune.seg_min_deposits_log2 = 28;
     *out = ctx;
     return DMANN_OK;
 }
@@ -425,6 +429,9 @@ dmann_status merge_tuning(dmann_ctx *ctx, const dmann_tuning &t, dmann_tuning &d
         return fail(ctx, DMANN_ERR_INVALID, "block_threads must be 128, 256 or 512");
     if (t.warp_max_pixels < 0 || t.blocks_per_sm < 0)
         return fail(ctx, DMANN_ERR_INVALID, "negative tuning value");
+    if (t.seg_min_deposits_log2 < 0 || t.seg_min_deposits_log2 > 62)
+        return fail(ctx, DMANN_ERR_INVALID, "seg_min_deposits_log2 must be in [1, 62]");
+    if (t.seg_min_deposits_log2 > 0) dst.seg_min_deposits_log2 = t.seg_min_deposits_log2;
     if (t.warp_max_pixels > 0) dst.warp_max_pixels = t.warp_max_pixels;
     if (t.blocks_per_sm > 0) dst.blocks_per_sm = t.blocks_per_sm;
     if (t.block_threads > 0) dst.block_threads = t.block_threads;
@@ -625,6 +632,49 @@ Accum make_accum(dmann_ctx *ctx) {
 // `used` stays false and the caller renders with the per-disc kernels.
 // Reads the item count back to the host (one synchronisation per chunk) to
 // size the item list and the segment count.
+// The segments of deposits from the per-octave histograms: n[c] items
+// ending at slot end[c] of the sorted list (k_seg_sort leaves each octave's
+// end slot), px[c] deposits.  Consecutive octaves are grouped while the
+// group spans at most kClassSpan octaves and budget deposits; an octave with
+// more than budget deposits is dealt round robin into ceil(px / budget)
+// segments of its own.  Class 0 (discs with no weighted deposits: single
+// pixels, zero flux) is one segment.  At most kSegMax segments: the budget
+// doubles until the plan fits.
+void plan_segments(const int *n, const int *end, const long long *px, long long budget,
+                   std::vector<SegSpan> &out) {
+    for (;;) {
+        out.clear();
+        if (n[0] > 0) out.push_back({(long long)end[0] - n[0], end[0], 1, 0});
+        int c0 = -1;
+        long long lo = 0, hi = 0, acc = 0;
+        auto close = [&] {
+            if (c0 >= 0) out.push_back({lo, hi, 1, 0});
+            c0 = -1;
+            acc = 0;
+        };
+        for (int c = 1; c < kClasses; ++c) {
+            if (n[c] == 0) continue;
+            const long long f = (long long)end[c] - n[c];
+            if (px[c] > budget) {
+                close();
+                const long long m = std::min<long long>(n[c], (px[c] + budget - 1) / budget);
+                for (long long k = 0; k < m; ++k) out.push_back({f, end[c], (int)m, (int)k});
+                continue;
+            }
+            if (c0 >= 0 && (c - c0 >= kClassSpan || acc + px[c] > budget)) close();
+            if (c0 < 0) {
+                c0 = c;
+                lo = f;
+            }
+            hi = end[c];
+            acc += px[c];
+        }
+        close();
+        if ((int)out.size() <= kSegMax) return;
+        budget *= 2;
+    }
+}
+
 dmann_status render_segmented(dmann_ctx *ctx, const DiscArgs &da, const dmann_tuning &tu, size_t N,
                               bool &used) {
     used = false;
@@ -632,50 +682,66 @@ dmann_status render_segmented(dmann_ctx *ctx, const DiscArgs &da, const dmann_tu
     const size_t n1 = N > 0 ? N : 1;
     if (!ensure_opt(ctx->seg_first, 8 * n1) || !ensure_opt(ctx->seg_nit, 4 * n1) ||
         !ensure_opt(ctx->seg_S, 8 * n1) || !ensure_opt(ctx->seg_px, 8 * n1) ||
-        !ensure_opt(ctx->seg_cls, 4 * 512))
+        !ensure_opt(ctx->seg_cls, kSegBufBytes))
         return DMANN_OK;
     cudaStream_t s = ctx->stream;
-    const int bt = tu.block_threads == 256 ? 256 : 128;
+    const int bt = tu.block_threads == 128 ? 128 : 256;
     SegArgs sg{};
     sg.disc_first = (long long *)ctx->seg_first.p;
     sg.disc_nitems = (int *)ctx->seg_nit.p;
     sg.disc_S = (double *)ctx->seg_S.p;
     sg.disc_px = (long long *)ctx->seg_px.p;
     sg.plane = (float *)ctx->plane32.p;
+    sg.cls = (int *)ctx->seg_cls.p;
+    sg.cls_px = (long long *)((char *)ctx->seg_cls.p + kSegClsBytes);
+    sg.seg_next = (unsigned long long *)((char *)ctx->seg_cls.p + kSegClsBytes + kSegClsPxBytes);
     CK(launch_hdr(da, ctx->num_sms, s));
     CK(launch_seg_count(da, sg, bt, ctx->num_sms, s));
     CK(cudaMemcpyAsync(ctx->h_seg, (long long *)ctx->ctr.p + C_SEG_ITEMS, 16, cudaMemcpyDeviceToHost, s));
     CK(cudaMemcpyAsync(ctx->h_seg + 2, (long long *)ctx->ctr.p + C_ADD_BLOCK, 8, cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
+    ctx->launches += 2;   // headers, item count
     const long long items = ctx->h_seg[0], est = ctx->h_seg[1], nblk = ctx->h_seg[2];
-    if (items > 0 && (!ensure_opt(ctx->seg_items, 8 * (size_t)items) ||
-                      !ensure_opt(ctx->seg_sorted, 8 * (size_t)items))) {
-        // no room for the item list: the per-disc kernels take the chunk
-        CK(launch_disc_comp(da, ctx->num_sms, tu.blocks_per_sm, tu.block_threads, s, ctx->evdm));
-        ctx->launches += 8;   // prep, scan, scatter, headers, item count, headers, block, warp
+    const int lg = tu.seg_min_deposits_log2 > 0 ? tu.seg_min_deposits_log2 : 28;
+    if (est < (1LL << lg) ||
+        (items > 0 && (!ensure_opt(ctx->seg_items, 8 * (size_t)items) ||
+                       !ensure_opt(ctx->seg_sorted, 8 * (size_t)items)))) {
+        // a small chunk (or no room for the item list): the per-disc kernels
+        // with FP64 deposits take it, on the headers already built
+        CK(launch_disc_comp(da, ctx->num_sms, tu.blocks_per_sm, tu.block_threads, s, ctx->evdm, false));
+        ctx->launches += 5;   // prep, scan, scatter, block, warp
         used = true;
         return DMANN_OK;
     }
     sg.items = (int2 *)ctx->seg_items.p;
     sg.sorted = (int2 *)ctx->seg_sorted.p;
-    sg.cls = (int *)ctx->seg_cls.p;
     sg.n_items = items;
-    const double per_pix = (double)est / (double)ctx->g.npix;
-    sg.n_seg = (int)std::min<double>(kSegMax, std::max(1.0, std::ceil(per_pix / kDepPerPix)));
     if (nblk > 0) {
         CK(cudaMemsetAsync(sg.disc_S, 0, 8 * (size_t)nblk, s));
         CK(cudaMemsetAsync(sg.disc_px, 0, 8 * (size_t)nblk, s));
     }
-    CK(cudaMemsetAsync(sg.cls, 0, 4 * 512, s));
+    CK(cudaMemsetAsync(ctx->seg_cls.p, 0, kSegBufBytes, s));
     CK(launch_seg_norm(da, sg, bt, ctx->num_sms, tu.blocks_per_sm, s));
     CK(cudaEventRecord(ctx->evp1, s));
-    CK(launch_seg_deposits(da, sg, bt, ctx->num_sms, tu.blocks_per_sm, ctx->g.npix, s));
+    CK(launch_seg_sort(da, sg, ctx->num_sms, s));
+    // the per-octave histograms plan the segments
+    long long *hc = ctx->h_seg + 4;
+    CK(cudaMemcpyAsync(hc, ctx->seg_cls.p, kSegClsBytes + kSegClsPxBytes, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    const int *cls_items = (const int *)hc;
+    const int *cls_end = cls_items + kClasses;
+    const long long *cls_px = (const long long *)((const char *)hc + kSegClsBytes);
+    const long long budget = std::max<long long>(1, (long long)ctx->g.npix * kDepPerPix);
+    std::vector<SegSpan> spans;
+    plan_segments(cls_items, cls_end, cls_px, budget, spans);
+    for (size_t k = 0; k < spans.size(); ++k)
+        CK(launch_seg_deposit(da, sg, spans[k], (int)k, bt, ctx->num_sms, tu.blocks_per_sm, ctx->g.npix, s));
     CK(cudaEventRecord(ctx->evdm, s));
     CK(launch_disc_comp_warp(da, ctx->num_sms, s));
     ctx->seg_timed = true;
-    // prep, scan, scatter, headers, item count, item fill, pass 1, item sort
-    // (3), K x (deposits, flush), warp class
-    ctx->launches += 11 + 2 * sg.n_seg;
+    // prep, scan, scatter, item fill, pass 1, item sort (3), segments x
+    // (deposits, flush), warp class
+    ctx->launches += 9 + 2 * (long long)spans.size();
     used = true;
     return DMANN_OK;
 }

@@ -372,8 +372,8 @@ cudaError_t launch_disc_comp_warp(const DiscArgs &a, int num_sms, cudaStream_t s
 size_t comp_hdr_bytes() { return sizeof(CompHdr); }
 
 cudaError_t launch_disc_comp(const DiscArgs &a, int num_sms, int blocks_per_sm, int block_threads,
-                             cudaStream_t s, cudaEvent_t mid) {
-    cudaError_t e = launch_hdr(a, num_sms, s);
+                             cudaStream_t s, cudaEvent_t mid, bool headers) {
+    cudaError_t e = headers ? launch_hdr(a, num_sms, s) : cudaSuccess;
     if (e != cudaSuccess) return e;
     if (block_threads == 128) e = launch_block<128, 192, 16>(a, num_sms, blocks_per_sm, s);
     else if (block_threads == 512) e = launch_block<512, 640, 4>(a, num_sms, blocks_per_sm, s);

@@ -39,21 +39,24 @@
 //
 // Deposits and segments.  A deposit w (F + Flo) is rounded once to FP32 and
 // added with red.global.add.f32 into an FP32 plane: half the L2 reduction
-// bytes of an FP64 deposit.  Two things keep those FP32 sums accurate.
-//   * Order.  The particles' deposit scales F span many decades, and a
-//     round-to-nearest FP32 sum drops any addend below half an ulp of the
-//     running total: small deposits arriving after large ones would be lost
-//     (a bias, always downwards).  After pass 1 the items are therefore
-//     sorted by the octave of F (a counting sort, k_seg_class .. k_seg_sort)
-//     and deposited in ascending order: a pixel's running total is then made
-//     of deposits no larger than the next one's disc scale, every addend
-//     stays many ulps above the total's rounding, and the rounding errors
-//     are unbiased.
-//   * Length.  The sorted items are dealt into K segments (item k to segment
-//     k mod K: each segment is an ascending sample of all discs); after each
-//     segment k_seg_flush adds the FP32 plane into the FP64 plane and clears
-//     it.  K is chosen so that a pixel takes about kDepPerPix FP32 additions
-//     per segment.
+// bytes of an FP64 deposit.  The deposits of a chunk are made in segments;
+// after each, k_seg_flush adds the FP32 plane into the FP64 plane and clears
+// it.  Two bounds on a segment keep its FP32 sums accurate:
+//   * Range.  The particles' deposit scales F span many decades, and a
+//     round-to-nearest FP32 sum drops any addend below half an ulp of its
+//     running total: small deposits landing on large totals would be lost,
+//     a bias that is always downwards.  After pass 1 the items are sorted by
+//     the octave of F (a counting sort, k_seg_class .. k_seg_sort); a segment
+//     holds items of at most kClassSpan consecutive octaves, so its smallest
+//     addend (w >= exp(-6) times its smallest F) stays above 2^-kClassSpan
+//     e^-6 / n of a pixel total of n additions -- many ulps for n in the
+//     hundreds, whatever order the concurrent blocks deposit in.
+//   * Length.  A segment holds about kDepPerPix deposits per pixel (an
+//     octave with more is dealt round robin into several segments), so a
+//     pixel's FP32 partial sums stay short and their rounding errors random.
+// The host plans the segments from the per-octave histograms (plan_segments).
+// Chunks too small for the L2 reduction rate to matter (a tunable threshold
+// on the estimated deposits) take the per-disc kernels with FP64 deposits.
 #include "comp_engine.cuh"
 
 namespace dmann {
@@ -61,7 +64,6 @@ namespace dmann {
 namespace {
 
 constexpr int kItemPx = 32768;   // pixels per work item (from the disc's cap-area estimate)
-constexpr int kClasses = 256;    // octaves of the deposit scale F (the item sort's keys)
 
 // One staged run: a ring's pixels inside the disc, contiguous in the map.
 struct alignas(16) SRun {
@@ -196,16 +198,16 @@ __device__ inline void seg_walk(SegSmem<RCH> &sm, int n, Body body, Done ring_do
 }
 
 // Claims the next work item for the block (thread 0: first + t stride for
-// the t-th claim) and stages its disc's header; false when the item range
-// is exhausted.
+// the t-th claim, below end) and stages its disc's header; false when the
+// item range is exhausted.
 template <int BT, int RCH>
 __device__ inline bool seg_claim(const DiscArgs &a, const SegArgs &sg, const int2 *items,
                                  SegSmem<RCH> &sm, unsigned long long *next, long long stride,
-                                 long long first, int2 &it) {
+                                 long long first, long long end, int2 &it) {
     if (threadIdx.x == 0) {
         const long long t = (long long)atomicAdd(next, 1ull);
         const long long k = first + t * stride;
-        sm.item = k < sg.n_items ? (int)k : -1;
+        sm.item = k < min(end, sg.n_items) ? (int)k : -1;
     }
     __syncthreads();
     const int k = sm.item;
@@ -266,7 +268,7 @@ __global__ void __launch_bounds__(BT, MINB) k_seg_norm(DiscArgs a, SegArgs sg) {
     __shared__ SegSmem<RCH> sm;
     int2 it;
     while (seg_claim<BT, RCH>(a, sg, sg.items, sm, (unsigned long long *)(a.ctr + C_SEG_NEXT_NORM), 1, 0,
-                              it)) {
+                              sg.n_items, it)) {
         int r0, n;
         item_rings(sm.h, it.y, r0, n);
         const bool poly = sm.h.ext.tier_x < 2 && sm.h.ext.tier_h < 2;
@@ -302,13 +304,13 @@ __device__ inline void dep_item(const DiscArgs &a, SegSmem<RCH> &sm, int r0, int
     __syncthreads();
 }
 
-// Segment s: items s, s + K, s + 2K, ... of the sorted list (ascending F).
+// One segment of deposits (its items of the sorted list, see SegSpan).
 template <int BT, int RCH, int MINB>
-__global__ void __launch_bounds__(BT, MINB) k_seg_dep(DiscArgs a, SegArgs sg, int s) {
+__global__ void __launch_bounds__(BT, MINB) k_seg_dep(DiscArgs a, SegArgs sg, SegSpan sp, int seg) {
     __shared__ SegSmem<RCH> sm;
     int2 it;
-    while (seg_claim<BT, RCH>(a, sg, sg.sorted, sm, (unsigned long long *)(a.ctr + C_SEG_NEXT_DEP + s),
-                              sg.n_seg, s, it)) {
+    while (seg_claim<BT, RCH>(a, sg, sg.sorted, sm, sg.seg_next + seg, sp.stride, sp.lo + sp.offset,
+                              sp.hi, it)) {
         const long long total = sg.disc_px[it.x];
         const double fs = sm.h.hdr.flux * a.f.inv_scale;
         if (total < 2) {   // genmap.cpp:125-128: the whole flux into the centre pixel
@@ -382,18 +384,27 @@ __device__ inline int seg_class(const DiscArgs &a, const SegArgs &sg, long long 
     return min(kClasses - 1, max(1, ilogb(F) + kClasses / 2));
 }
 
-// Items per class (the histogram, sg.cls[0 .. kClasses)).
+// Items and pixels per class (sg.cls[0 .. kClasses), sg.cls_px).
 __global__ void __launch_bounds__(256) k_seg_class(DiscArgs a, SegArgs sg) {
     __shared__ int hist[kClasses];
-    for (int i = threadIdx.x; i < kClasses; i += blockDim.x) hist[i] = 0;
+    __shared__ unsigned long long px[kClasses];
+    for (int i = threadIdx.x; i < kClasses; i += blockDim.x) {
+        hist[i] = 0;
+        px[i] = 0;
+    }
     __syncthreads();
     const long long nblk = a.ctr[C_ADD_BLOCK];
     const long long stride = (long long)gridDim.x * blockDim.x;
-    for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < nblk; q += stride)
-        atomicAdd(&hist[seg_class(a, sg, q)], sg.disc_nitems[q]);
+    for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < nblk; q += stride) {
+        const int c = seg_class(a, sg, q);
+        atomicAdd(&hist[c], sg.disc_nitems[q]);
+        atomicAdd(&px[c], (unsigned long long)sg.disc_px[q]);
+    }
     __syncthreads();
-    for (int i = threadIdx.x; i < kClasses; i += blockDim.x)
+    for (int i = threadIdx.x; i < kClasses; i += blockDim.x) {
         if (hist[i]) atomicAdd(sg.cls + i, hist[i]);
+        if (px[i]) atomicAdd((unsigned long long *)sg.cls_px + i, px[i]);
+    }
 }
 
 // Exclusive scan of the class histogram into the classes' first slots
@@ -461,30 +472,14 @@ cudaError_t launch_norm(const DiscArgs &a, const SegArgs &sg, int num_sms, int b
     return cudaGetLastError();
 }
 
-// The item list sorted by the octave of each disc's deposit scale.
-cudaError_t launch_sort(const DiscArgs &a, const SegArgs &sg, int num_sms, cudaStream_t s) {
-    k_seg_class<<<num_sms * 4, 256, 0, s>>>(a, sg);
+template <int BT, int RCH, int MINB>
+cudaError_t launch_deposit(const DiscArgs &a, const SegArgs &sg, const SegSpan &span, int seg, int num_sms,
+                           int blocks_per_sm, int npix, cudaStream_t s) {
+    k_seg_dep<BT, RCH, MINB><<<grid_of<BT, RCH, MINB>(num_sms, blocks_per_sm), BT, 0, s>>>(a, sg, span, seg);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
-    k_seg_cscan<<<1, kClasses, 0, s>>>(sg);
-    if ((e = cudaGetLastError()) != cudaSuccess) return e;
-    k_seg_sort<<<num_sms * 8, 256, 0, s>>>(a, sg);
+    k_seg_flush<<<num_sms * 8, 256, 0, s>>>(sg.plane, a.acc.acc64, npix / 4);
     return cudaGetLastError();
-}
-
-template <int BT, int RCH, int MINB>
-cudaError_t launch_deposits(const DiscArgs &a, const SegArgs &sg, int num_sms, int blocks_per_sm, int npix,
-                            cudaStream_t s) {
-    const int grid = grid_of<BT, RCH, MINB>(num_sms, blocks_per_sm);
-    cudaError_t e = launch_sort(a, sg, num_sms, s);
-    if (e != cudaSuccess) return e;
-    for (int seg = 0; seg < sg.n_seg; seg++) {
-        k_seg_dep<BT, RCH, MINB><<<grid, BT, 0, s>>>(a, sg, seg);
-        if ((e = cudaGetLastError()) != cudaSuccess) return e;
-        k_seg_flush<<<num_sms * 8, 256, 0, s>>>(sg.plane, a.acc.acc64, npix / 4);
-        if ((e = cudaGetLastError()) != cudaSuccess) return e;
-    }
-    return cudaSuccess;
 }
 
 }  // namespace
@@ -502,10 +497,22 @@ cudaError_t launch_seg_norm(const DiscArgs &a, const SegArgs &sg, int block_thre
     return launch_norm<128, 128, 16>(a, sg, num_sms, blocks_per_sm, s);
 }
 
-cudaError_t launch_seg_deposits(const DiscArgs &a, const SegArgs &sg, int block_threads, int num_sms,
-                                int blocks_per_sm, int npix, cudaStream_t s) {
-    if (block_threads == 256) return launch_deposits<256, 256, 8>(a, sg, num_sms, blocks_per_sm, npix, s);
-    return launch_deposits<128, 128, 16>(a, sg, num_sms, blocks_per_sm, npix, s);
+cudaError_t launch_seg_sort(const DiscArgs &a, const SegArgs &sg, int num_sms, cudaStream_t s) {
+    k_seg_class<<<num_sms * 4, 256, 0, s>>>(a, sg);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    k_seg_cscan<<<1, kClasses, 0, s>>>(sg);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    k_seg_sort<<<num_sms * 8, 256, 0, s>>>(a, sg);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_seg_deposit(const DiscArgs &a, const SegArgs &sg, const SegSpan &span, int seg,
+                               int block_threads, int num_sms, int blocks_per_sm, int npix,
+                               cudaStream_t s) {
+    if (block_threads == 256)
+        return launch_deposit<256, 256, 8>(a, sg, span, seg, num_sms, blocks_per_sm, npix, s);
+    return launch_deposit<128, 128, 16>(a, sg, span, seg, num_sms, blocks_per_sm, npix, s);
 }
 
 }  // namespace dmann

@@ -21,10 +21,19 @@ constexpr int kKeys = kBuckets * kCells;
 // Device counters (int64).  The first six accumulate over every chunk of
 // a map; the C_ADD_* ones describe the chunk being added and are reset for
 // each chunk.
-// Segmented render (disc_seg.cu): at most kSegMax segments of the FP32
-// plane per chunk, each taking about kDepPerPix FP32 additions per pixel.
-constexpr int kSegMax = 32;
+// Segmented render (disc_seg.cu).  The items are sorted into kClasses
+// octaves of their disc's deposit scale; a segment of deposits spans at most
+// kClassSpan consecutive octaves and about kDepPerPix FP32 additions per
+// pixel (kSegMax segments at most per chunk).  Chunks whose estimated
+// deposits are below 2^seg_min_deposits_log2 (a tunable) deposit in FP64.
+constexpr int kClasses = 256;
+constexpr int kClassSpan = 2;
 constexpr int kDepPerPix = 512;
+constexpr int kSegMax = 1024;
+// The segment buffer (SegArgs.cls, cls_px, seg_next, in this order).
+constexpr size_t kSegClsBytes = 2 * 4 * kClasses;
+constexpr size_t kSegClsPxBytes = 8 * kClasses;
+constexpr size_t kSegBufBytes = kSegClsBytes + kSegClsPxBytes + 8 * kSegMax;
 
 enum Ctr {
     C_KEPT = 0, C_SINGLE, C_DISC, C_DISC_BLOCK, C_DEPOSITS, C_INVALID,
@@ -32,8 +41,7 @@ enum Ctr {
     C_SEG_ITEMS,       // work items of the chunk's block-class discs
     C_SEG_EST,         // their estimated pixels (cap areas)
     C_SEG_NEXT_NORM,   // items claimed by pass 1
-    C_SEG_NEXT_DEP,    // kSegMax counters: items claimed by each segment
-    C_COUNT = C_SEG_NEXT_DEP + kSegMax
+    C_COUNT
 };
 constexpr int kCtrChunkFirst = C_ADD_DISC;
 
@@ -105,14 +113,22 @@ struct DiscArgs {
 struct SegArgs {
     int2 *items;              // (queue slot, item index within its disc), queue order
     int2 *sorted;             // the same items in ascending octave of the disc's F
-    int *cls;                 // [2 x 256]: items per octave, then each octave's first slot
+    int *cls;                 // [2 kClasses]: items per octave, then each octave's first slot
+    long long *cls_px;        // [kClasses]: pixels (deposits) per octave
+    unsigned long long *seg_next;   // [kSegMax]: items claimed by each segment
     long long n_items;
     long long *disc_first;    // per block-class disc: its first item
     int *disc_nitems;         //   its item count
     double *disc_S;           //   the sum of its weights (pass 1; zeroed by the caller)
     long long *disc_px;       //   its pixel count (pass 1; zeroed by the caller)
     float *plane;             // FP32 deposit plane, npix floats, zero between segments
-    int n_seg;                // segments K (1 .. kSegMax)
+};
+
+// One segment of deposits: items lo + offset, lo + offset + stride, ... below
+// hi of the sorted list.
+struct SegSpan {
+    long long lo, hi;
+    int stride, offset;
 };
 
 // prep.cu
@@ -132,22 +148,26 @@ cudaError_t launch_disc_plain(const DiscArgs &a, int num_sms, int blocks_per_sm,
                               cudaEvent_t mid);
 // block_threads: 128, 256 or 512 (the compensated block kernel's shape;
 // anything else means 256).
+// headers = false: the disc headers were already built (launch_hdr).
 cudaError_t launch_disc_comp(const DiscArgs &a, int num_sms, int blocks_per_sm, int block_threads,
-                             cudaStream_t s, cudaEvent_t mid);
+                             cudaStream_t s, cudaEvent_t mid, bool headers = true);
 size_t comp_hdr_bytes();
 // the headers of every queued disc (k_comp_hdr; nothing when a.chdr is null)
 cudaError_t launch_hdr(const DiscArgs &a, int num_sms, cudaStream_t s);
 // the warp-per-particle compensated kernel alone (the warp class)
 cudaError_t launch_disc_comp_warp(const DiscArgs &a, int num_sms, cudaStream_t s);
 // disc_seg.cu: the item count of every block-class disc (needs the headers);
-// the item list and pass 1; the n_seg segments of deposits, each followed by
-// its flush.  block_threads 128 or 256 picks the block shape.
+// the item list and pass 1; the items sorted by octave (with the per-octave
+// histograms); one segment of deposits followed by its flush.
+// block_threads 128 or 256 picks the block shape.
 cudaError_t launch_seg_count(const DiscArgs &a, const SegArgs &sg, int block_threads, int num_sms,
                              cudaStream_t s);
 cudaError_t launch_seg_norm(const DiscArgs &a, const SegArgs &sg, int block_threads, int num_sms,
                             int blocks_per_sm, cudaStream_t s);
-cudaError_t launch_seg_deposits(const DiscArgs &a, const SegArgs &sg, int block_threads, int num_sms,
-                                int blocks_per_sm, int npix, cudaStream_t s);
+cudaError_t launch_seg_sort(const DiscArgs &a, const SegArgs &sg, int num_sms, cudaStream_t s);
+cudaError_t launch_seg_deposit(const DiscArgs &a, const SegArgs &sg, const SegSpan &span, int seg,
+                               int block_threads, int num_sms, int blocks_per_sm, int npix,
+                               cudaStream_t s);
 // adjoint.cu: gradients of the plain-form map for dL/dmap = gmap; grad is
 // [6][n] (x, y, z, m, rho, h); oacc[12] (zeroed by the caller) receives
 // sum_i dL/du_i and dL/drot (row-major).  Needs the prep outputs (with cls)

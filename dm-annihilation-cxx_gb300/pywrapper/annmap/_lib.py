@@ -41,7 +41,7 @@ class Stats(C.Structure):
 class Tuning(C.Structure):
     _fields_ = [("warp_max_pixels", C.c_int64), ("block_threads", C.c_int32),
                 ("blocks_per_sm", C.c_int32), ("ring_chunk", C.c_int32),
-                ("reserved", C.c_int32 * 3)]
+                ("seg_min_deposits_log2", C.c_int32), ("reserved", C.c_int32 * 2)]
 
 
 _LIB = None

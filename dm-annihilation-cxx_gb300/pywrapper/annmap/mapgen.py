@@ -127,7 +127,8 @@ class Renderer:
 
     def set_tuning(self, nside: int | None = None, **kw):
         """Default tuning, or the entry for maps of ``nside``
-        (warp_max_pixels, block_threads, blocks_per_sm)."""
+        (warp_max_pixels, block_threads, blocks_per_sm,
+        seg_min_deposits_log2)."""
         t = _lib.Tuning()
         for k, v in kw.items():
             setattr(t, k, v)

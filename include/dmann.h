@@ -108,12 +108,13 @@ typedef struct {
     double pass1_ms;       /* compensated form, block class of the last chunk: from the
                               disc kernels' start to the end of the weight sums (headers,
                               work items, pass 1) */
-    double pass2_ms;       /* the deposit segments and their flushes */
+    double pass2_ms;       /* the item sort, the deposit segments and their flushes
+                              (both 0 when the chunk deposited in FP64) */
 } dmann_stats;
 
 /* Tunables (set by the annmap autotuner; zero fields keep the current
  * values).  Defaults: warp_max_pixels 1024, block_threads 256, blocks_per_sm
- * 0 (as many as fit). */
+ * 0 (as many as fit), seg_min_deposits_log2 28. */
 typedef struct {
     int64_t warp_max_pixels;   /* footprint-class bin edge: discs estimated up
                                   to this many pixels go warp-per-particle,
@@ -124,7 +125,13 @@ typedef struct {
                                   block kernel, capped by occupancy; 0 = max */
     int32_t ring_chunk;        /* read only: rings staged per pass for the
                                   block shape (192, 384, 640) */
-    int32_t reserved[3];
+    int32_t seg_min_deposits_log2;  /* compensated form: a chunk whose block-
+                                  class discs are estimated to make at least
+                                  2^this many deposits takes the segmented
+                                  render (FP32 deposits flushed into the FP64
+                                  plane per segment, 128 or 256 threads);
+                                  smaller chunks deposit in FP64.  1 .. 62 */
+    int32_t reserved[2];
 } dmann_tuning;
 
 /* ---- lifetime ---- */

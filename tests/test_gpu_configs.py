@@ -12,7 +12,10 @@ every host thread.
     dmann_render_batch call, on a 2^17-particle prefix;
   * the large-map set (NFW + 500 subhalos, particles within 0.5 kpc of the
     observer) at Nside 4096: an i.i.d. sample of it, with one disc covering
-    the whole sky.
+    the whole sky;
+  * the segmented render (FP32 deposits in segments of at most two octaves of
+    the deposit scale, flushed into the FP64 plane) forced onto the samples
+    above, which by default are small enough to deposit in FP64.
 
 Tolerances: per-pixel relative error median <= 1e-5, max <= 1e-4 and total
 flux <= 1e-9 relative for the compensated form; for the plain form the
@@ -132,15 +135,10 @@ def test_config_batched_three_observers(rend):
         check(out.cpu().numpy(), ref, tot, o.dOmega, COMP, f"batched observer Nside {ns}", ns)
 
 
-def test_config_large_map_sample_ns4096(rend):
-    """An i.i.d. sample of the large-map configuration: 65,536 particles of the
-    134,217,728-particle NFW + 500 subhalo set (its particle mass and
-    densities), 4 of them within 0.5 kpc of the observer, at Nside 4096
-    (201,326,592 pixels), both forms."""
+def large_map_sample():
     m = 4.1e3 * (1 << 24) / (1 << 27)
     P = synth.nfw_halo(1 << 16, seed=20240013, n_sub=500, particle_mass=m, near_observer=4,
                        n_total=1 << 27)
-    nside = 4096
     # one near-observer particle moved to 0.02 kpc of the observer: its disc
     # (radius 2 h / d > pi) covers the whole sky
     obs = np.array(P.obs_pos)
@@ -152,6 +150,15 @@ def test_config_large_map_sample_ns4096(rend):
     P.x[k], P.y[k], P.z[k] = (obs + 0.02 / math.sqrt(3.0)).astype(np.float32)
     d[k] = np.linalg.norm(np.array([P.x[k], P.y[k], P.z[k]], np.float64) - obs)
     assert 2 * P.h[k] / d[k] > math.pi
+    return P, 4096
+
+
+def test_config_large_map_sample_ns4096(rend):
+    """An i.i.d. sample of the large-map configuration: 65,536 particles of the
+    134,217,728-particle NFW + 500 subhalo set (its particle mass and
+    densities), 4 of them within 0.5 kpc of the observer, at Nside 4096
+    (201,326,592 pixels), both forms."""
+    P, nside = large_map_sample()
     o, ref, ost, tot = oracle_map(P, nside)
     rend.set_params(annmap.Parameters.for_synthetic(P, nside))
     for prec in (COMP, PLAIN):
@@ -159,3 +166,31 @@ def test_config_large_map_sample_ns4096(rend):
         check(got, ref, tot, o.dOmega, prec, f"large-map sample precision {prec}", nside)
         assert rend.stats()["deposits"] == ost["deposits"]
         assert np.all(got > 0)   # the all-sky disc reaches every pixel
+
+
+@pytest.mark.parametrize("case", ["nfw1m_ns512", "nfw16m_prefix", "large_map_sample"])
+@pytest.mark.parametrize("block_threads", [128, 256])
+def test_segmented_render_forced(case, block_threads):
+    """The segmented render taken on chunks of any size (its threshold at 2
+    estimated deposits), both block shapes: the same bounds against the
+    oracle, the same deposits, and the pass timings that only the segmented
+    render records."""
+    if case == "nfw1m_ns512":
+        P, nside = synth.workload("nfw1m_ns512")
+    elif case == "nfw16m_prefix":
+        P, nside = synth.workload("nfw16m_sub100_ns2048")
+        P = P.subset(slice(0, 1 << 16))
+    else:
+        P, nside = large_map_sample()
+    o, ref, ost, tot = oracle_map(P, nside)
+    r = annmap.Renderer(0)
+    try:
+        r.set_tuning(seg_min_deposits_log2=1, block_threads=block_threads)
+        r.set_params(annmap.Parameters.for_synthetic(P, nside))
+        got = r.render(P.as_dict(), nside, COMP)
+        st = r.stats()
+        check(got, ref, tot, o.dOmega, COMP, f"segmented {case} {block_threads} threads", nside)
+        assert st["deposits"] == ost["deposits"]
+        assert st["pass2_ms"] > 0.0
+    finally:
+        r.close()
