@@ -47,6 +47,8 @@ def parse():
                     "the particles (particles get fatter: same halo mass)")
     ap.add_argument("--subset", type=int, default=0, help="render only the first N particles of the "
                     "full (shuffled) workload: same per-particle disc statistics")
+    ap.add_argument("--nside", type=int, default=0, help="render at this Nside instead of the "
+                    "workload's (the overlap density, deposits per pixel, does not depend on it)")
     ap.add_argument("--plain-scale", type=float, default=1.0 / 64)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-extras", action="store_true", help="skip plain form, e2e and CPU legs")
@@ -239,7 +241,8 @@ def cpu_oracle_run(P, nside, seconds, threads=None):
 
 def bench_config(args, n, nside):
     """The workload description both arms print (identical in the two lines)."""
-    return {"workload": args.workload + (f" (first {n} particles)" if args.subset else ""),
+    return {"workload": args.workload + (f" (first {n} particles)" if args.subset else "")
+            + (f" at Nside {nside}" if args.nside else ""),
             "particles": n, "nside": nside,
             "l2": f"no flush: inputs {24 * n / 1e6:.0f} MB + map/planes "
                   f"{16 * 12 * nside * nside / 1e6:.0f} MB > 126 MB L2"}
@@ -258,6 +261,7 @@ def run_reference(args, ws, rank):
     import oracle as O
     from annmap import synth
     P, nside = synth.workload(args.workload, scale=args.scale)
+    nside = args.nside or nside
     if args.subset:
         P = P.subset(slice(0, args.subset))
     n = len(P)
@@ -312,6 +316,7 @@ def run_gb300(args, ws, rank, local):
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
     P, nside = synth.workload(args.workload, scale=args.scale)
+    nside = args.nside or nside
     if args.subset:
         P = P.subset(slice(0, args.subset))
     n = len(P)
