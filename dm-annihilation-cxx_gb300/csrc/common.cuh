@@ -267,6 +267,15 @@ __device__ inline void red_add_f64(double *addr, double v) {
 __device__ inline void red_add_f32(float *addr, float v) {
     asm volatile("red.global.add.f32 [%0], %1;" ::"l"(addr), "f"(v));
 }
+// Vector reductions (sm_90+): two or four consecutive floats, the address
+// aligned to 8 or 16 bytes.
+__device__ inline void red_add_v2_f32(float *addr, float a, float b) {
+    asm volatile("red.global.add.v2.f32 [%0], {%1, %2};" ::"l"(addr), "f"(a), "f"(b));
+}
+__device__ inline void red_add_v4_f32(float *addr, float a, float b, float c, float d) {
+    asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(addr), "f"(a), "f"(b), "f"(c),
+                 "f"(d));
+}
 __device__ inline float atom_add_f32(float *addr, float v) {
     float old;
     asm volatile("atom.global.add.f32 %0, [%1], %2;" : "=f"(old) : "l"(addr), "f"(v));

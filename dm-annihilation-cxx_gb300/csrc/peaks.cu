@@ -9,6 +9,9 @@
 //   DMANN_PEAK_RED_F32   red.global.add.f32 (no return value)
 //   DMANN_PEAK_RED_F64   red.global.add.f64
 //   DMANN_PEAK_RED_U64   red.global.add.u64 (an atomicAdd whose value is unused)
+//   DMANN_PEAK_RED_F32X2 red.global.add.v2.f32, DMANN_PEAK_RED_F32X4
+//                        red.global.add.v4.f32: a lane adds to two or four
+//                        consecutive floats (rates counted in floats)
 //   DMANN_PEAK_COMP_F32  a two-plane compensated FP32 deposit (the disc
 //                        kernels' earlier form): atom.global.add.f32 that
 //                        returns the old value, the exact TwoSum error and a
@@ -41,6 +44,10 @@ __global__ void __launch_bounds__(256) k_sweep(void *buf, long long n, int reps,
                 red_add_f32((float *)buf + i, v);
             } else if (KIND == DMANN_PEAK_RED_F64) {
                 red_add_f64((double *)buf + i, (double)v);
+            } else if (KIND == DMANN_PEAK_RED_F32X2) {
+                red_add_v2_f32((float *)buf + 2 * i, v, v);
+            } else if (KIND == DMANN_PEAK_RED_F32X4) {
+                red_add_v4_f32((float *)buf + 4 * i, v, v, v, v);
             } else if (KIND == DMANN_PEAK_RED_U64) {
                 atomicAdd((unsigned long long *)buf + i, (unsigned long long)(v * 1048576.0f));
             } else {
@@ -60,7 +67,7 @@ extern "C" dmann_status dmann_measure_l2_red(int device, int kind, int64_t bytes
     if (!ops_per_s || reps < 1 || bytes < (1 << 20) || bytes > ((int64_t)1 << 34))
         return DMANN_ERR_INVALID;
     if (kind != DMANN_PEAK_RED_F32 && kind != DMANN_PEAK_RED_F64 && kind != DMANN_PEAK_COMP_F32 &&
-        kind != DMANN_PEAK_RED_U64)
+        kind != DMANN_PEAK_RED_U64 && kind != DMANN_PEAK_RED_F32X2 && kind != DMANN_PEAK_RED_F32X4)
         return DMANN_ERR_INVALID;
     if (cudaSetDevice(device) != cudaSuccess) {
         cudaGetLastError();
@@ -75,7 +82,8 @@ extern "C" dmann_status dmann_measure_l2_red(int device, int kind, int64_t bytes
         return DMANN_ERR_NOMEM;
     }
     const long long elem = (kind == DMANN_PEAK_RED_F64 || kind == DMANN_PEAK_RED_U64) ? 8 : 4;
-    const long long n = kind == DMANN_PEAK_COMP_F32 ? bytes / (2 * elem) : bytes / elem;
+    const long long width = kind == DMANN_PEAK_RED_F32X2 ? 2 : kind == DMANN_PEAK_RED_F32X4 ? 4 : 1;
+    const long long n = kind == DMANN_PEAK_COMP_F32 ? bytes / (2 * elem) : bytes / (elem * width);
     if (kind == DMANN_PEAK_COMP_F32 && n > 0x7fffffffLL) {
         cudaFree(buf);
         return DMANN_ERR_INVALID;
@@ -96,6 +104,10 @@ extern "C" dmann_status dmann_measure_l2_red(int device, int kind, int64_t bytes
             if (kind == DMANN_PEAK_RED_F32) k_sweep<DMANN_PEAK_RED_F32><<<grid, 256, 0, s>>>(buf, n, r, v);
             else if (kind == DMANN_PEAK_RED_F64) k_sweep<DMANN_PEAK_RED_F64><<<grid, 256, 0, s>>>(buf, n, r, v);
             else if (kind == DMANN_PEAK_RED_U64) k_sweep<DMANN_PEAK_RED_U64><<<grid, 256, 0, s>>>(buf, n, r, v);
+            else if (kind == DMANN_PEAK_RED_F32X2)
+                k_sweep<DMANN_PEAK_RED_F32X2><<<grid, 256, 0, s>>>(buf, n, r, v);
+            else if (kind == DMANN_PEAK_RED_F32X4)
+                k_sweep<DMANN_PEAK_RED_F32X4><<<grid, 256, 0, s>>>(buf, n, r, v);
             else k_sweep<DMANN_PEAK_COMP_F32><<<grid, 256, 0, s>>>(buf, n, r, v);
         };
         launch(1);  // warm-up
@@ -107,7 +119,7 @@ extern "C" dmann_status dmann_measure_l2_red(int device, int kind, int64_t bytes
             !(ms > 0.0f))
             st = DMANN_ERR_CUDA;
         else
-            *ops_per_s = (double)n * reps / (ms * 1e-3);
+            *ops_per_s = (double)n * width * reps / (ms * 1e-3);
     }
     cudaGetLastError();
     if (e0) cudaEventDestroy(e0);

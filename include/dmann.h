@@ -327,13 +327,15 @@ typedef enum {
     DMANN_PEAK_COMP_F32 = 2,  /* a two-plane compensated FP32 deposit: returning
                                  FP32 atomic add, exact TwoSum error, FP32 red of
                                  the error */
-    DMANN_PEAK_RED_U64 = 3    /* red.global.add.u64 */
+    DMANN_PEAK_RED_U64 = 3,   /* red.global.add.u64 */
+    DMANN_PEAK_RED_F32X2 = 4, /* red.global.add.v2.f32: two consecutive floats per lane */
+    DMANN_PEAK_RED_F32X4 = 5  /* red.global.add.v4.f32: four consecutive floats per lane */
 } dmann_peak_kind;
-/* No reference counterpart.  Measures the rate (operations per second) of
- * one kind of global reduction on `device`: a grid of 8 blocks per SM sweeps
- * an array of `bytes` (1 MiB .. 16 GiB; a 400 MB array exceeds the L2) with
- * lanes of a warp on consecutive elements, `reps` times, after one warm-up
- * sweep.  The deposit scatter of the projection is bound by this rate (one
+/* No reference counterpart.  Measures the rate (operations per second; for
+ * the vector kinds, floats added per second) of one kind of global reduction
+ * on `device`: a grid of 8 blocks per SM sweeps an array of `bytes` (1 MiB ..
+ * 16 GiB; a 400 MB array exceeds the L2) with lanes of a warp on consecutive
+ * elements, `reps` times, after one warm-up sweep.  The deposit scatter of the projection is bound by this rate (one
  * reduction per algorithmic deposit). */
 dmann_status dmann_measure_l2_red(int device, int kind, int64_t bytes, int reps,
                                   double *ops_per_s);
