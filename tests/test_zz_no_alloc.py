@@ -48,6 +48,11 @@ def test_noalloc_matches_render_on_two_calls():
         par = annmap.Parameters.for_synthetic(P, nside)
         dev = {k: torch.from_numpy(v).cuda() for k, v in P.as_dict().items()}
         with annmap.Renderer(0) as r:
+            # the no-alloc entry point deposits in FP64 (the per-disc kernels);
+            # so does the context's render below 2^62 estimated deposits
+            # (this halo's fat particles would otherwise take the segmented
+            # render, whose FP32 deposits differ by their own rounding)
+            r.set_tuning(seg_min_deposits_log2=62)
             r.set_params(par)
             ref = r.render(P.as_dict(), nside, annmap.COMP_F32)
         out = torch.full((12 * nside * nside,), 7.0, dtype=torch.float64, device="cuda")
