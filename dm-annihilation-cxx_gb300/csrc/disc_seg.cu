@@ -64,7 +64,6 @@ namespace dmann {
 namespace {
 
 constexpr int kItemPx = 32768;   // pixels per work item (from the disc's cap-area estimate)
-constexpr int kQuad = 4;         // pixels per lane step: one 16-byte four-float reduction
 
 // One staged run: a ring's pixels inside the disc, contiguous in the map.
 struct alignas(16) SRun {
@@ -72,22 +71,19 @@ struct alignas(16) SRun {
     float d0h, steph;       // x(j) = d0h + j steph, half the azimuth offset of pixel j
     float c0, c1, c2, c3;   // polynomial path: E = c0 + y (c1 + y (c2 + y (c3 + y c4)));
     float c4;               // general path: c0 = A, c1 = B, c2 = A2 (see Run)
-    int qfirst;             // the run's first quad in the item's quad space
-    int pad0, pad1;
+    int more;               // the ring continues in the next slot (it wrapped)
+    float pad0, pad1;
 };
-static_assert(sizeof(SRun) == 48, "SRun is read as three 16-byte words");
+static_assert(sizeof(SRun) == 48, "SRun is copied as three 16-byte words");
 
-// The item's runs, two slots per ring (the second holds the ring's
-// continuation where its pixel index wraps, else nothing), and a sentinel.
 template <int RCH>
 struct SegSmem {
-    SRun run[2 * RCH + 1];
+    SRun run[2 * RCH];      // two slots per ring (the second only where it wraps)
     CompHdr h;
     float2 red2[32];        // per-warp two-float sums
     int cnt_red[32];
-    int q_red[32];
     double F;               // flux * inv_scale / S (pass 2)
-    int nquad;              // quads of the item
+    int next_run;           // rings claimed so far (dynamic claims of the walk)
     int item;               // the claimed item
 };
 
@@ -115,71 +111,45 @@ struct Blk {
     static constexpr int kWarps = BT / 32;
 };
 
-// Quads of a run: the 16-byte-aligned groups of four map pixels it touches.
-__device__ __forceinline__ int run_quads(int pix0, int cnt) {
-    return cnt > 0 ? ((pix0 + cnt + kQuad - 1) / kQuad - pix0 / kQuad) : 0;
-}
-
-// Stages rings r0 .. r0+n-1 (n <= BT) of the staged particle as runs, one
-// thread per ring, and numbers their quads (a block-wide exclusive scan:
-// the item's quad space).  Returns the pixel count of the rings (all
-// threads); sm.nquad holds the quad count.
+// Stages rings r0 .. r0+n-1 of the staged particle as runs (one thread per
+// ring); returns the pixel count of those rings (all threads).
 template <int BT, int RCH>
 __device__ inline int seg_build(const DiscArgs &a, SegSmem<RCH> &sm, int r0, int n, bool poly) {
-    static_assert(RCH == BT, "one ring per thread");
-    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
-    Run r[2] = {};
-    float co[5] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
     int c = 0;
-    if (t < n) {
-        c = make_runs(a, sm.h.hdr, sm.h.ch, sm.h.ext.tier_h == 2, r0 + t, r);
-        co[0] = r[0].A;
-        co[1] = r[0].B;
-        co[2] = r[0].A2;
-        if (poly && c > 0) poly_coeffs(r[0].A, r[0].B, sm.h.ext.nK, sm.h.ext.tier_h, co);
-    }
-    const int nq0 = run_quads(r[0].pix0, r[0].cnt), nq1 = run_quads(r[1].pix0, r[1].cnt);
-    int wq;
-    const int ex = warp_excl_scan(nq0 + nq1, wq);
-    const int wc = __reduce_add_sync(0xffffffffu, c);
-    if (lane == 0) {
-        sm.q_red[warp] = wq;
-        sm.cnt_red[warp] = wc;
-    }
-    __syncthreads();
-    int base = 0, total = 0, nquad = 0;
-    for (int k = 0; k < Blk<BT>::kWarps; k++) {
-        base += k < warp ? sm.q_red[k] : 0;
-        nquad += sm.q_red[k];
-        total += sm.cnt_red[k];
-    }
-    if (t < n) {
+    const bool need_a2 = sm.h.ext.tier_h == 2;
+    for (int i = threadIdx.x; i < n; i += BT) {
+        Run r[2] = {};
+        const int k = make_runs(a, sm.h.hdr, sm.h.ch, need_a2, r0 + i, r);
+        c += k;
+        float co[5] = {r[0].A, r[0].B, r[0].A2, 0.0f, 0.0f};
+        if (poly && k > 0) poly_coeffs(r[0].A, r[0].B, sm.h.ext.nK, sm.h.ext.tier_h, co);
 #pragma unroll
-        for (int k = 0; k < 2; k++) {
+        for (int s = 0; s < 2; s++) {
             SRun o;
-            o.pix0 = r[k].pix0;
-            o.cnt = r[k].cnt;
-            o.d0h = r[k].d0h;
-            o.steph = r[k].steph;
+            o.pix0 = r[s].pix0;
+            o.cnt = r[s].cnt;
+            o.d0h = r[s].d0h;
+            o.steph = r[s].steph;
             o.c0 = co[0];
             o.c1 = co[1];
             o.c2 = co[2];
             o.c3 = co[3];
             o.c4 = co[4];
-            o.qfirst = base + ex + (k ? nq0 : 0);
-            o.pad0 = o.pad1 = 0;
-            sm.run[2 * t + k] = o;
+            o.more = r[s].more;
+            o.pad0 = o.pad1 = 0.0f;
+            sm.run[2 * i + s] = o;
         }
     }
-    if (t == 0) {
-        sm.run[2 * n].qfirst = 0x7fffffff;   // sentinel: stops the walk's slot search
-        sm.nquad = nquad;
-    }
+    c = __reduce_add_sync(0xffffffffu, c);
+    if ((threadIdx.x & 31) == 0) sm.cnt_red[threadIdx.x >> 5] = c;
+    if (threadIdx.x == 0) sm.next_run = 0;
     __syncthreads();
-    return total;
+    c = 0;
+    for (int k = 0; k < Blk<BT>::kWarps; k++) c += sm.cnt_red[k];
+    return c;
 }
 
-// The weights of pixels jj = (j, j + 1) of run r.
+// The weights of pixels jj = (j, j + 32) of run r.
 template <bool POLY>
 __device__ __forceinline__ float2 seg_weight2(const Ext &e, const SRun &r, float2 jj) {
     if constexpr (POLY) {
@@ -204,52 +174,26 @@ __device__ __forceinline__ float2 seg_weight2(const Ext &e, const SRun &r, float
     }
 }
 
-// The four weights of quad j0 .. j0+3 of run r (local pixel indices; those
-// outside [0, cnt) are 0).
-template <bool POLY>
-__device__ __forceinline__ void quad_weights(const Ext &e, const SRun &r, int j0, float2 &wa, float2 &wb) {
-    const float jf = (float)j0;
-    wa = seg_weight2<POLY>(e, r, add2(f2(jf), make_float2(0.0f, 1.0f)));
-    wb = seg_weight2<POLY>(e, r, add2(f2(jf), make_float2(2.0f, 3.0f)));
-    const unsigned n = (unsigned)r.cnt;
-    wa.x = (unsigned)j0 < n ? wa.x : 0.0f;
-    wa.y = (unsigned)(j0 + 1) < n ? wa.y : 0.0f;
-    wb.x = (unsigned)(j0 + 2) < n ? wb.x : 0.0f;
-    wb.y = (unsigned)(j0 + 3) < n ? wb.y : 0.0f;
-}
-
-// The walk over the staged item's quad space.  The quads are cut into
-// chunks of 32; each warp takes a contiguous range of chunks, lane l the
-// l-th quad of each chunk, so a warp's lanes touch consecutive quads (64
-// contiguous bytes of the map per 4 lanes within a run).  Each lane follows
-// its slot forward from the warp's starting slot.  body(run, j0) gets the
-// local index of the quad's first map pixel (negative for a run's first
-// quad when the run starts inside it); fold(chunk) runs on every lane of
-// the warp after each chunk.
-template <int BT, int RCH, class Body, class Fold>
-__device__ inline void quad_walk(SegSmem<RCH> &sm, int nslots, Body body, Fold fold) {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int nq = sm.nquad;
-    const int nch = (nq + 31) >> 5;
-    const int ch0 = nch * warp / Blk<BT>::kWarps, ch1 = nch * (warp + 1) / Blk<BT>::kWarps;
-    if (ch0 >= ch1) return;
-    // the last slot whose first quad is at or before the warp's first quad
-    int lo = 0, hi = nslots;
-    const int g0 = ch0 << 5;
-    while (hi - lo > 1) {
-        const int mid = (lo + hi) >> 1;
-        if (sm.run[mid].qfirst <= g0) lo = mid;
-        else hi = mid;
-    }
-    int s = lo;
-    for (int ch = ch0; ch < ch1; ch++) {
-        const int q = (ch << 5) + lane;
-        if (q < nq) {
-            while (sm.run[s + 1].qfirst <= q) s++;
-            const SRun r = sm.run[s];
-            body(r, ((r.pix0 / kQuad + (q - r.qfirst)) * kQuad) - r.pix0);
+// Warps claim whole rings (both slots) of the staged item and call
+// body(run, j, second) for pixels j and j + 32 (second: j + 32 is inside).
+// ring_done() runs on every lane after each ring.
+template <int RCH, class Body, class Done>
+__device__ inline void seg_walk(SegSmem<RCH> &sm, int n, Body body, Done ring_done) {
+    const int lane = threadIdx.x & 31;
+    int q = 0;
+    if (lane == 0) q = atomicAdd(&sm.next_run, 1);
+    q = __shfl_sync(0xffffffffu, q, 0);
+    while (q < n) {
+        int qn = 0;
+        if (lane == 0) qn = atomicAdd(&sm.next_run, 1);
+        const SRun r = sm.run[2 * q];
+        for (int j = lane; j < r.cnt; j += 64) body(r, j, j + 32 < r.cnt);
+        if (r.more) {
+            const SRun r2 = sm.run[2 * q + 1];
+            for (int j = lane; j < r2.cnt; j += 64) body(r2, j, j + 32 < r2.cnt);
         }
-        fold(ch);
+        ring_done();
+        q = __shfl_sync(0xffffffffu, qn, 0);
     }
 }
 
@@ -291,28 +235,22 @@ __device__ inline void norm_item(const DiscArgs &a, SegSmem<RCH> &sm, int r0, in
                                  float &S_lo, int &total) {
     const Ext e = sm.h.ext;
     total = seg_build<BT, RCH>(a, sm, r0, n, POLY);
-    float s = 0.0f, c = 0.0f;   // this lane's two-float sum of its partials
-    float2 part = f2(0.0f);     // plain FP32 partial of at most four quads
-    quad_walk<BT, RCH>(
-        sm, 2 * n,
-        [&](const SRun &r, int j0) {
-            float2 wa, wb;
-            quad_weights<POLY>(e, r, j0, wa, wb);
-            part = add2(part, add2(wa, wb));
+    float s = 0.0f, c = 0.0f;   // this lane's two-float sum of its run partials
+    float2 part = f2(0.0f);
+    seg_walk<RCH>(
+        sm, n,
+        [&](const SRun &r, int j, bool second) {
+            const float jf = (float)j;
+            float2 w = seg_weight2<POLY>(e, r, make_float2(jf, jf + 32.0f));
+            if (!second) w.y = 0.0f;
+            part = add2(part, w);
         },
-        [&](int ch) {
-            if ((ch & 3) == 3) {
-                float err;
-                s = two_sum(s, part.x + part.y, err);
-                c += err;
-                part = f2(0.0f);
-            }
+        [&]() {
+            float err;
+            s = two_sum(s, part.x + part.y, err);
+            c += err;
+            part = f2(0.0f);
         });
-    {
-        float err;
-        s = two_sum(s, part.x + part.y, err);
-        c += err;
-    }
     warp_sum_ff(s, c);
     if ((threadIdx.x & 31) == 0) sm.red2[threadIdx.x >> 5] = make_float2(s, c);
     __syncthreads();
@@ -347,24 +285,22 @@ __global__ void __launch_bounds__(BT, MINB) k_seg_norm(DiscArgs a, SegArgs sg) {
     }
 }
 
-// Pass 2 of one item: each lane deposits its quads with one four-float
-// reduction each (the quad's pixels outside the run add zero).
 template <int BT, int RCH, bool POLY>
 __device__ inline void dep_item(const DiscArgs &a, SegSmem<RCH> &sm, int r0, int n, float F, float Flo,
                                 float *plane) {
     const Ext e = sm.h.ext;
     seg_build<BT, RCH>(a, sm, r0, n, POLY);
-    quad_walk<BT, RCH>(
-        sm, 2 * n,
-        [&](const SRun &r, int j0) {
-            float2 wa, wb;
-            quad_weights<POLY>(e, r, j0, wa, wb);
-            // w (F + Flo), rounded once
-            const float2 pa = fma2(wa, f2(F), mul2(wa, f2(Flo)));
-            const float2 pb = fma2(wb, f2(F), mul2(wb, f2(Flo)));
-            red_add_v4_f32(plane + (r.pix0 + j0), pa.x, pa.y, pb.x, pb.y);
+    seg_walk<RCH>(
+        sm, n,
+        [&](const SRun &r, int j, bool second) {
+            const float jf = (float)j;
+            const float2 w = seg_weight2<POLY>(e, r, make_float2(jf, jf + 32.0f));
+            const float2 p = fma2(w, f2(F), mul2(w, f2(Flo)));   // w (F + Flo), rounded once
+            float *const m = plane + (r.pix0 + j);
+            red_add_f32(m, p.x);
+            if (second) red_add_f32(m + 32, p.y);
         },
-        [](int) {});
+        []() {});
     __syncthreads();
 }
 

@@ -9,8 +9,16 @@ numpy and checked exhaustively or on many samples (no GPU).
     within 1.8e-8 / 2.1e-8 (resp. their stated bounds) of the FP64
     functions at the tier limits;
   * ks - 1 is exact in FP32 for 1 <= ks < 2^24 (the offset normalisation
-    sum), and Dekker's two-float division recovers a / b to ~2^-44.
+    sum), and Dekker's two-float division recovers a / b to ~2^-44;
+  * the large discs' fitted asin^2(sqrt h) polynomial (g_near2 in
+    csrc/comp_engine.cuh, its coefficients read from the source) is within
+    2e-8 relative of asin^2(sqrt h) on [0, 1/2] in exact arithmetic (with
+    the FP32-rounded coefficients) and within 1.5e-7 (two FP32 ulps) when
+    evaluated in FP32.
 """
+import os
+import re
+
 import numpy as np
 
 
@@ -109,3 +117,33 @@ def test_two_float_division():
         exact = (float(ah) + float(al)) / (float(bh) + float(bl))
         worst = max(worst, abs(float(hi) + float(lo) - exact) / exact)
     assert worst < 2.0 ** -42, worst
+
+
+def _g_near_coefficients():
+    """Q's coefficients, highest degree first, as g_near2 evaluates them."""
+    src = open(os.path.join(os.path.dirname(__file__), "..", "dm-annihilation-cxx_gb300", "csrc",
+                            "comp_engine.cuh")).read()
+    body = src[src.index("float2 g_near2("):]
+    body = body[:body.index("return mul2(h, q);")]
+    nums = [float(v) for v in re.findall(r"f2\((-?[0-9.]+(?:e-?[0-9]+)?)f\)", body)]
+    assert len(nums) == 9, nums
+    return nums
+
+
+def test_large_disc_asin2_polynomial():
+    c = _g_near_coefficients()
+    h = np.linspace(0.0, 0.5, 50001)[1:]
+    ref = np.arcsin(np.sqrt(h)) ** 2
+    q = np.zeros_like(h)
+    for ck in c:
+        q = q * h + ck
+    assert np.max(np.abs(h * q - ref) / ref) < 2e-8
+    # FP32 Horner with fused steps (one rounding per FMA), then g = h * q
+    h32 = h.astype(np.float32)
+    q32 = np.full_like(h32, np.float32(c[0]))
+    for ck in c[1:]:
+        q32 = (q32.astype(np.float64) * h32.astype(np.float64) + np.float64(np.float32(ck))).astype(np.float32)
+    g32 = (h32 * q32).astype(np.float64)
+    ref32 = np.arcsin(np.sqrt(h32.astype(np.float64))) ** 2
+    assert np.max(np.abs(g32 - ref32) / ref32) < 1.5e-7
+    assert c[-1] == 1.0   # Q(0) = 1: g = h + O(h^2) near the disc centre
