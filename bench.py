@@ -159,32 +159,36 @@ def profile_traffic():
     return None
 
 
-def measure_l2_red(device, nbytes=400_000_000):
+def measure_l2_red(device, plane_floats):
     """Live L2 reduction rates (operations/s) of the library's own sweep
-    microbenchmark over a 400 MB array: FP32 red (the compensated form's
-    deposit) and FP64 red (the plain form's)."""
+    microbenchmark: FP32 red (the compensated form's deposit) over an array
+    the size of the FP32 deposit plane (the footprint the deposits land
+    in), and for reference FP32 and FP64 red over 400 MB."""
     import ctypes as C
     from annmap import _lib
     L = _lib.load()
     out = {}
-    for name, kind, reps in (("red_f32", 0, 20), ("red_f64", 1, 20)):
+    plane = max(1 << 20, 4 * int(plane_floats))
+    for name, kind, nbytes in (("red_f32", 0, plane), ("red_f32_400mb", 0, 400_000_000),
+                               ("red_f64_400mb", 1, 400_000_000)):
         v = C.c_double()
-        st = L.dmann_measure_l2_red(int(device), kind, int(nbytes), reps, C.byref(v))
+        st = L.dmann_measure_l2_red(int(device), kind, int(nbytes), 20, C.byref(v))
         out[name] = v.value if st == 0 else None
+    out["plane_bytes"] = plane
     return out
 
 
 FP32_FLOPS_PER_WEIGHT = 12   # x (FMA), y = x^2, 4 Horner FMAs, the sum: 2 + 1 + 8 + 1
 
 
-def roofline(device, deposits, pass1_ms, pass2_ms):
+def roofline(device, deposits, pass1_ms, pass2_ms, npix):
     """The deposit pass's roofline on its binding resource, the L2 reduction
     units: each algorithmic deposit is one FP32 reduction (4 B) into the
     map's FP32 plane, against the library's live red.global.add.f32 sweep.
     Beside it the same bytes against measured HBM, and pass 1 (weight sums:
     FP32 arithmetic, no memory traffic to speak of) against the nominal FP32
     rate of the FMA pipes."""
-    l2 = measure_l2_red(device)
+    l2 = measure_l2_red(device, npix)
     hbm, hbm_src = measured_peaks()
     red_bytes = 4.0 * deposits
     s2, s1 = pass2_ms / 1e3, pass1_ms / 1e3
@@ -195,15 +199,16 @@ def roofline(device, deposits, pass1_ms, pass2_ms):
     p1_tflops = deposits * FP32_FLOPS_PER_WEIGHT / s1 / 1e12
     return {"bound": "l2_red", "kernel": "k_seg_dep (deposit segments)", "achieved": achieved,
             "peak": peak, "unit": "GB/s", "frac": achieved / peak if peak else None,
-            "peak_source": (f"measured here: red.global.add.f32 sweep over 400 MB "
-                            f"({l2['red_f32']:.3e} reductions/s)") if l2["red_f32"] else "unavailable",
+            "peak_source": (f"measured here: red.global.add.f32 sweep over the deposit plane's "
+                            f"{l2['plane_bytes'] / 1e6:.0f} MB ({l2['red_f32']:.3e} reductions/s)")
+            if l2["red_f32"] else "unavailable",
             "traffic": (traffic["dram_bytes_per_deposit"] * deposits) if traffic else None,
             "traffic_source": traffic.get("capture") if traffic else None,
             "algorithmic_bytes": red_bytes,
             "basis": "4 B FP32 reduction per algorithmic deposit / deposit-pass time (CUDA events)",
             "hbm": {"achieved": achieved, "peak": hbm, "frac": achieved / hbm,
                     "peak_source": hbm_src + " (MEASURED_PEAKS hbm_gbs)"},
-            "red_f64_sweep_ops": l2["red_f64"],
+            "sweeps_400mb": {"red_f32": l2["red_f32_400mb"], "red_f64": l2["red_f64_400mb"]},
             "pass1": {"kernel": "k_seg_norm (weight sums)", "ms": pass1_ms, "weights_per_s": deposits / s1,
                       "fp32_flops_per_weight": FP32_FLOPS_PER_WEIGHT, "achieved_tflops": p1_tflops,
                       "peak_tflops": nominal_fp32,
@@ -391,7 +396,7 @@ def run_gb300(args, ws, rank, local):
 
     line["stage_ms"].update({"pass1": statistics.mean(p1_ms), "pass2": statistics.mean(p2_ms)})
     line["roofline"] = roofline(local, step_stats["deposits"], statistics.mean(p1_ms),
-                                statistics.mean(p2_ms))
+                                statistics.mean(p2_ms), npix)
 
     if not args.no_extras and rank == 0:
         # plain FP64 form on a prefix (the plain form is FP64-throughput bound)

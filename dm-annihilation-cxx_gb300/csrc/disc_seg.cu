@@ -149,7 +149,7 @@ __device__ inline int seg_build(const DiscArgs &a, SegSmem<RCH> &sm, int r0, int
     return c;
 }
 
-// The weights of pixels jj = (j, j + 32) of run r.
+// The weights of pixels jj = (j, j + S) of run r.
 template <bool POLY>
 __device__ __forceinline__ float2 seg_weight2(const Ext &e, const SRun &r, float2 jj) {
     if constexpr (POLY) {
@@ -174,28 +174,42 @@ __device__ __forceinline__ float2 seg_weight2(const Ext &e, const SRun &r, float
     }
 }
 
-// Warps claim whole rings (both slots) of the staged item and call
-// body(run, j, second) for pixels j and j + 32 (second: j + 32 is inside).
-// ring_done() runs on every lane after each ring.
-template <int RCH, class Body, class Done>
+// Warps claim 32 / S consecutive rings (both slots of each) of the staged
+// item at a time, one ring per group of S lanes, and call
+// body(run, j, second) for pixels j and j + S of the ring (second: j + S is
+// inside), so the per-ring work of the walk (the claim, the run's loads,
+// the loop set-up, ring_done) is shared by the rings a warp walks together;
+// neighbouring rings of a disc have similar lengths, so the groups finish
+// together.  The S lanes of a group touch S consecutive pixels (S floats of
+// the map per deposit instruction).  ring_done() runs on every lane after
+// each claim.
+template <int RCH, int S, class Body, class Done>
 __device__ inline void seg_walk(SegSmem<RCH> &sm, int n, Body body, Done ring_done) {
-    const int lane = threadIdx.x & 31;
-    int q = 0;
-    if (lane == 0) q = atomicAdd(&sm.next_run, 1);
-    q = __shfl_sync(0xffffffffu, q, 0);
-    while (q < n) {
+    static_assert(S == 8 || S == 16 || S == 32, "lanes per ring");
+    constexpr int G = 32 / S;
+    const int lane = threadIdx.x & 31, sl = lane % S;
+    int q0 = 0;
+    if (lane == 0) q0 = atomicAdd(&sm.next_run, G);
+    q0 = __shfl_sync(0xffffffffu, q0, 0);
+    while (q0 < n) {
         int qn = 0;
-        if (lane == 0) qn = atomicAdd(&sm.next_run, 1);
-        const SRun r = sm.run[2 * q];
-        for (int j = lane; j < r.cnt; j += 64) body(r, j, j + 32 < r.cnt);
-        if (r.more) {
-            const SRun r2 = sm.run[2 * q + 1];
-            for (int j = lane; j < r2.cnt; j += 64) body(r2, j, j + 32 < r2.cnt);
+        if (lane == 0) qn = atomicAdd(&sm.next_run, G);
+        const int q = q0 + lane / S;
+        if (q < n) {
+            const SRun r = sm.run[2 * q];
+            for (int j = sl; j < r.cnt; j += 2 * S) body(r, j, j + S < r.cnt);
+            if (r.more) {
+                const SRun r2 = sm.run[2 * q + 1];
+                for (int j = sl; j < r2.cnt; j += 2 * S) body(r2, j, j + S < r2.cnt);
+            }
         }
         ring_done();
-        q = __shfl_sync(0xffffffffu, qn, 0);
+        q0 = __shfl_sync(0xffffffffu, qn, 0);
     }
 }
+
+constexpr int kNormLanes = 8;    // lanes per ring in pass 1 (weights only)
+constexpr int kDepLanes = 16;    // lanes per ring in pass 2 (16 floats of the map per reduction)
 
 // Claims the next work item for the block (thread 0: first + t stride for
 // the t-th claim, below end) and stages its disc's header; false when the
@@ -237,11 +251,11 @@ __device__ inline void norm_item(const DiscArgs &a, SegSmem<RCH> &sm, int r0, in
     total = seg_build<BT, RCH>(a, sm, r0, n, POLY);
     float s = 0.0f, c = 0.0f;   // this lane's two-float sum of its run partials
     float2 part = f2(0.0f);
-    seg_walk<RCH>(
+    seg_walk<RCH, kNormLanes>(
         sm, n,
         [&](const SRun &r, int j, bool second) {
             const float jf = (float)j;
-            float2 w = seg_weight2<POLY>(e, r, make_float2(jf, jf + 32.0f));
+            float2 w = seg_weight2<POLY>(e, r, make_float2(jf, jf + (float)kNormLanes));
             if (!second) w.y = 0.0f;
             part = add2(part, w);
         },
@@ -290,15 +304,15 @@ __device__ inline void dep_item(const DiscArgs &a, SegSmem<RCH> &sm, int r0, int
                                 float *plane) {
     const Ext e = sm.h.ext;
     seg_build<BT, RCH>(a, sm, r0, n, POLY);
-    seg_walk<RCH>(
+    seg_walk<RCH, kDepLanes>(
         sm, n,
         [&](const SRun &r, int j, bool second) {
             const float jf = (float)j;
-            const float2 w = seg_weight2<POLY>(e, r, make_float2(jf, jf + 32.0f));
+            const float2 w = seg_weight2<POLY>(e, r, make_float2(jf, jf + (float)kDepLanes));
             const float2 p = fma2(w, f2(F), mul2(w, f2(Flo)));   // w (F + Flo), rounded once
             float *const m = plane + (r.pix0 + j);
             red_add_f32(m, p.x);
-            if (second) red_add_f32(m + 32, p.y);
+            if (second) red_add_f32(m + kDepLanes, p.y);
         },
         []() {});
     __syncthreads();
