@@ -483,7 +483,9 @@ def run_gb300(args, ws, rank, local):
 def bench_batched(dev):
     """64 observers on the 8 kpc sphere, Nside cycling 256/512/1024, all maps
     of the 8,388,608-particle set rendered by one dmann_render_batch call
-    (one CUDA graph; inputs and maps on the device)."""
+    (one CUDA graph, captured by the warm-up call and relaunched by the timed
+    one; inputs and maps on the device), against the same 64 maps rendered
+    one dmann_render call at a time."""
     import torch
     import annmap
     from annmap import synth
@@ -501,17 +503,34 @@ def bench_batched(dev):
     r.set_params(par)
     from annmap import autotune
     tuned = autotune.tune_nsides(r, dparts, nsides, annmap.COMP_F32, sample=1 << 20, reps=1)
-    r.render_batch(dparts, frames, nsides, annmap.COMP_F32, outs=outs)   # warm-up
+    t0 = time.perf_counter()
+    r.render_batch(dparts, frames, nsides, annmap.COMP_F32, outs=outs)   # warm-up: captures the graph
     torch.cuda.synchronize()
+    t_capture = time.perf_counter() - t0
     t0 = time.perf_counter()
     r.render_batch(dparts, frames, nsides, annmap.COMP_F32, outs=outs)
     torch.cuda.synchronize()
     dt = time.perf_counter() - t0
+    st = r.stats()
+    # the same maps one render call each (same tuning, device inputs and maps)
+    singles = []
+    for (rot, opos), ns, out in zip(frames, nsides, outs):
+        r.set_frame(rot, opos)
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        r.render(dparts, ns, annmap.COMP_F32, out=out)
+        torch.cuda.synchronize()
+        singles.append(time.perf_counter() - t1)
     r.close()
     return {"workload": "nfw8m_sub50_batched", "particles": len(P), "observers": len(obs),
             "nsides": sorted(set(nsides)), "form": "compensated FP32", "seconds": dt,
             "maps_per_s": len(obs) / dt, "particle_maps_per_s": len(P) * len(obs) / dt,
-            "launch": "one CUDA graph (dmann_render_batch, device maps)",
+            "deposits": st["deposits"], "deposits_per_s": st["deposits"] / dt,
+            "graph_ms": st["kernel_ms"], "launches": st["launches"],
+            "first_call_seconds": t_capture,
+            "sum_of_single_renders_seconds": sum(singles),
+            "speedup_vs_single_renders": sum(singles) / dt,
+            "launch": "one CUDA graph (dmann_render_batch, device maps), kept across calls",
             "tuning": {str(k): v["best"] for k, v in tuned.items()}}
 
 

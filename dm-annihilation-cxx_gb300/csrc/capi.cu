@@ -5,6 +5,7 @@
 //   -> disc kernels (block per large disc, warp per small disc)
 //   -> final map pass (divide by dOmega, optional accumulate).
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -63,9 +64,13 @@ struct dmann_ctx {
     // weight sums and pixel counts, and the FP32 deposit plane
     DevBuf seg_items, seg_sorted, seg_cls, seg_first, seg_nit, seg_S, seg_px, plane32;
     bool seg_plane = false;       // plane32 holds a zeroed plane for the open map
-    // pinned: item count, estimated pixels, block-class discs (4 slots), then
-    // the per-octave item counts, first slots and pixels (the segment plan)
-    long long *h_seg = nullptr;
+    // dmann_render_batch: the instantiated graph of the last batch of device
+    // maps and the parameters it was captured with (relaunched when a batch
+    // repeats them), and the batch's counters summed over its observers
+    cudaGraphExec_t batch_exec = nullptr;
+    std::vector<char> batch_key;
+    long long batch_launches = 0;
+    DevBuf bstats;
     // halo cores of the ann_core_nosom law (dmann_set_halo_cores)
     DevBuf halo_f, halo_cells, corr;
     HaloGrid halo{};
@@ -116,12 +121,17 @@ int block_bucket_min(const dmann_tuning &t) {
 // each, with headroom for slowly growing chunks).  Optional: without them
 // the kernels compute each header themselves -- slower, the same results --
 // so a failed allocation is not an error.
+// Incremented by every (re)allocation of a context buffer: a captured batch
+// graph holds buffer addresses, so a batch is recaptured after any.
+std::atomic<unsigned long long> g_alloc_gen{0};
+
 void reserve_headers(dmann_ctx *ctx, size_t n) {
     const size_t bytes = comp_hdr_bytes() * (n > 0 ? n : 1);
     if (ctx->chdr.bytes >= bytes) return;
     if (ctx->chdr.p) cudaFree(ctx->chdr.p);
     ctx->chdr.p = nullptr;
     ctx->chdr.bytes = 0;
+    ++g_alloc_gen;
     for (size_t want : {bytes + bytes / 8, bytes}) {
         if (cudaMalloc(&ctx->chdr.p, want) == cudaSuccess) {
             ctx->chdr.bytes = want;
@@ -136,6 +146,7 @@ void reserve_headers(dmann_ctx *ctx, size_t n) {
 // error (the caller takes a path that does without it).
 bool ensure_opt(DevBuf &b, size_t bytes) {
     if (b.bytes >= bytes) return true;
+    ++g_alloc_gen;
     if (b.p) cudaFree(b.p);
     b.p = nullptr;
     b.bytes = 0;
@@ -157,6 +168,7 @@ CompHdr *headers_for(const dmann_ctx *ctx, size_t n) {
 
 dmann_status ensure(dmann_ctx *ctx, DevBuf &b, size_t bytes) {
     if (b.bytes >= bytes) return DMANN_OK;
+    ++g_alloc_gen;
     if (b.p) {
         cudaFree(b.p);
         b.p = nullptr;
@@ -270,7 +282,7 @@ dmann_status collect_stats(dmann_ctx *ctx) {
         ctx->stats.disc_warp_ms = ctx->stats.disc_ms - ms;
     }
     ctx->stats.pass1_ms = ctx->stats.pass2_ms = 0.0;
-    if (ctx->seg_timed) {
+    if (ctx->seg_timed && ctx->h_ctr[C_SEG_MODE] == 1) {   // the last chunk was segmented
         CK(cudaEventElapsedTime(&ms, ctx->evd0, ctx->evp1));
         ctx->stats.pass1_ms = ms;
         CK(cudaEventElapsedTime(&ms, ctx->evp1, ctx->evdm));
@@ -314,9 +326,7 @@ dmann_status dmann_create(dmann_ctx **out, int device) {
         cudaEventCreate(&ctx->ev0) != cudaSuccess || cudaEventCreate(&ctx->ev1) != cudaSuccess ||
         cudaEventCreate(&ctx->evd0) != cudaSuccess || cudaEventCreate(&ctx->evd1) != cudaSuccess ||
         cudaEventCreate(&ctx->evdm) != cudaSuccess || cudaEventCreate(&ctx->evp1) != cudaSuccess ||
-        cudaHostAlloc((void **)&ctx->h_ctr, 8 * (C_COUNT + 1 + 12), cudaHostAllocDefault) != cudaSuccess ||
-        cudaHostAlloc((void **)&ctx->h_seg, 8 * 4 + kSegClsBytes + kSegClsPxBytes, cudaHostAllocDefault) !=
-            cudaSuccess) {
+        cudaHostAlloc((void **)&ctx->h_ctr, 8 * (C_COUNT + 1 + 12), cudaHostAllocDefault) != cudaSuccess) {
         cudaGetLastError();
         delete ctx;
         return DMANN_ERR_CUDA;
@@ -344,7 +354,8 @@ void dmann_destroy(dmann_ctx *ctx) {
                       &ctx->cls, &ctx->oacc, &ctx->grad, &ctx->halo_f, &ctx->halo_cells,
                       &ctx->corr, &ctx->chdr, &ctx->core_gln, &ctx->seg_items, &ctx->seg_sorted,
                       &ctx->seg_cls, &ctx->seg_first,
-                      &ctx->seg_nit, &ctx->seg_S, &ctx->seg_px, &ctx->plane32};
+                      &ctx->seg_nit, &ctx->seg_S, &ctx->seg_px, &ctx->plane32, &ctx->bstats};
+    if (ctx->batch_exec) cudaGraphExecDestroy(ctx->batch_exec);
     for (DevBuf *b : bufs)
         if (b->p) cudaFree(b->p);
     for (auto &kv : ctx->rings) {
@@ -356,7 +367,6 @@ void dmann_destroy(dmann_ctx *ctx) {
         cudaFree(kv.second.step32);
     }
     if (ctx->h_ctr) cudaFreeHost(ctx->h_ctr);
-    if (ctx->h_seg) cudaFreeHost(ctx->h_seg);
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
     if (ctx->evd0) cudaEventDestroy(ctx->evd0);
     if (ctx->evd1) cudaEventDestroy(ctx->evd1);
@@ -627,121 +637,68 @@ Accum make_accum(dmann_ctx *ctx) {
 }
 
 // The compensated form's block-class discs in work items and segments
-// (disc_seg.cu), then the warp class with the per-disc kernel.  Needs the
-// disc headers, the FP32 plane and the item buffers; without any of them
-// `used` stays false and the caller renders with the per-disc kernels.
-// Reads the item count back to the host (one synchronisation per chunk) to
-// size the item list and the segment count.
-// The segments of deposits from the per-octave histograms: n[c] items
-// ending at slot end[c] of the sorted list (k_seg_sort leaves each octave's
-// end slot), px[c] deposits.  Consecutive octaves are grouped while the
-// group spans at most kClassSpan octaves and budget deposits; an octave with
-// more than budget deposits is dealt round robin into ceil(px / budget)
-// segments of its own.  Class 0 (discs with no weighted deposits: single
-// pixels, zero flux) is one segment.  At most kSegMax segments: the budget
-// doubles until the plan fits.
-void plan_segments(const int *n, const int *end, const long long *px, long long budget,
-                   std::vector<SegSpan> &out) {
-    for (;;) {
-        out.clear();
-        if (n[0] > 0) out.push_back({(long long)end[0] - n[0], end[0], 1, 0});
-        int c0 = -1;
-        long long lo = 0, hi = 0, acc = 0;
-        auto close = [&] {
-            if (c0 >= 0) out.push_back({lo, hi, 1, 0});
-            c0 = -1;
-            acc = 0;
-        };
-        for (int c = 1; c < kClasses; ++c) {
-            if (n[c] == 0) continue;
-            const long long f = (long long)end[c] - n[c];
-            if (px[c] > budget) {
-                close();
-                const long long m = std::min<long long>(n[c], (px[c] + budget - 1) / budget);
-                for (long long k = 0; k < m; ++k) out.push_back({f, end[c], (int)m, (int)k});
-                continue;
-            }
-            if (c0 >= 0 && (c - c0 >= kClassSpan || acc + px[c] > budget)) close();
-            if (c0 < 0) {
-                c0 = c;
-                lo = f;
-            }
-            hi = end[c];
-            acc += px[c];
-        }
-        close();
-        if ((int)out.size() <= kSegMax) return;
-        budget *= 2;
-    }
+// (disc_seg.cu), then the warp class with the per-disc kernel.  The item
+// list holds up to 4 N + 2^20 items; the device decides per chunk whether
+// the segmented render or the per-disc block kernel (FP64 deposits) takes
+// the block class, and both are launched -- the one not chosen returns at
+// once -- so nothing here waits for the device and the sequence can be
+// captured in a graph.  Needs the disc headers, the FP32 plane and the item
+// buffers; without them `used` stays false and the caller renders with the
+// per-disc kernels alone.
+size_t seg_capacity(size_t n) { return 4 * (n > 0 ? n : 1) + ((size_t)1 << 20); }
+
+// The segmented render's buffers for chunks of n particles (optional: false
+// when an allocation fails; nothing is allocated when they are big enough).
+bool reserve_seg(dmann_ctx *ctx, size_t n) {
+    const size_t n1 = n > 0 ? n : 1, cap = seg_capacity(n);
+    return ensure_opt(ctx->seg_first, 8 * n1) && ensure_opt(ctx->seg_nit, 4 * n1) &&
+           ensure_opt(ctx->seg_S, 8 * n1) && ensure_opt(ctx->seg_px, 8 * n1) &&
+           ensure_opt(ctx->seg_cls, kSegBufBytes) && ensure_opt(ctx->seg_items, 8 * cap) &&
+           ensure_opt(ctx->seg_sorted, 8 * cap);
 }
 
 dmann_status render_segmented(dmann_ctx *ctx, const DiscArgs &da, const dmann_tuning &tu, size_t N,
-                              bool &used) {
+                              bool &used, bool timed = true) {
     used = false;
-    if (!da.chdr || !ctx->seg_plane) return DMANN_OK;
-    const size_t n1 = N > 0 ? N : 1;
-    if (!ensure_opt(ctx->seg_first, 8 * n1) || !ensure_opt(ctx->seg_nit, 4 * n1) ||
-        !ensure_opt(ctx->seg_S, 8 * n1) || !ensure_opt(ctx->seg_px, 8 * n1) ||
-        !ensure_opt(ctx->seg_cls, kSegBufBytes))
-        return DMANN_OK;
+    if (!da.chdr || !ctx->seg_plane || !reserve_seg(ctx, N)) return DMANN_OK;
+    const size_t cap = seg_capacity(N);
     cudaStream_t s = ctx->stream;
     const int bt = tu.block_threads == 128 ? 128 : 256;
+    const int lg = tu.seg_min_deposits_log2 > 0 ? tu.seg_min_deposits_log2 : 28;
+    char *buf = (char *)ctx->seg_cls.p;
     SegArgs sg{};
+    sg.items = (int2 *)ctx->seg_items.p;
+    sg.sorted = (int2 *)ctx->seg_sorted.p;
+    sg.cap = (long long)cap;
+    sg.cls = (int *)buf;
+    sg.cls_px = (long long *)(buf + kSegClsBytes);
+    sg.seg_next = (unsigned long long *)(buf + kSegClsBytes + kSegClsPxBytes);
+    sg.spans = (SegSpan *)(buf + kSegClsBytes + kSegClsPxBytes + kSegNextBytes);
+    sg.ctl = (int *)(buf + kSegClsBytes + kSegClsPxBytes + kSegNextBytes + kSegSpanBytes);
+    sg.min_est = 1LL << lg;
+    sg.budget = (long long)ctx->g.npix * kDepPerPix;
     sg.disc_first = (long long *)ctx->seg_first.p;
     sg.disc_nitems = (int *)ctx->seg_nit.p;
     sg.disc_S = (double *)ctx->seg_S.p;
     sg.disc_px = (long long *)ctx->seg_px.p;
     sg.plane = (float *)ctx->plane32.p;
-    sg.cls = (int *)ctx->seg_cls.p;
-    sg.cls_px = (long long *)((char *)ctx->seg_cls.p + kSegClsBytes);
-    sg.seg_next = (unsigned long long *)((char *)ctx->seg_cls.p + kSegClsBytes + kSegClsPxBytes);
+    CK(cudaMemsetAsync(buf, 0, kSegBufBytes, s));
     CK(launch_hdr(da, ctx->num_sms, s));
     CK(launch_seg_count(da, sg, bt, ctx->num_sms, s));
-    CK(cudaMemcpyAsync(ctx->h_seg, (long long *)ctx->ctr.p + C_SEG_ITEMS, 16, cudaMemcpyDeviceToHost, s));
-    CK(cudaMemcpyAsync(ctx->h_seg + 2, (long long *)ctx->ctr.p + C_ADD_BLOCK, 8, cudaMemcpyDeviceToHost, s));
-    CK(cudaStreamSynchronize(s));
-    ctx->launches += 2;   // headers, item count
-    const long long items = ctx->h_seg[0], est = ctx->h_seg[1], nblk = ctx->h_seg[2];
-    const int lg = tu.seg_min_deposits_log2 > 0 ? tu.seg_min_deposits_log2 : 28;
-    if (est < (1LL << lg) ||
-        (items > 0 && (!ensure_opt(ctx->seg_items, 8 * (size_t)items) ||
-                       !ensure_opt(ctx->seg_sorted, 8 * (size_t)items)))) {
-        // a small chunk (or no room for the item list): the per-disc kernels
-        // with FP64 deposits take it, on the headers already built
-        CK(launch_disc_comp(da, ctx->num_sms, tu.blocks_per_sm, tu.block_threads, s, ctx->evdm, false));
-        ctx->launches += 5;   // prep, scan, scatter, block, warp
-        used = true;
-        return DMANN_OK;
-    }
-    sg.items = (int2 *)ctx->seg_items.p;
-    sg.sorted = (int2 *)ctx->seg_sorted.p;
-    sg.n_items = items;
-    if (nblk > 0) {
-        CK(cudaMemsetAsync(sg.disc_S, 0, 8 * (size_t)nblk, s));
-        CK(cudaMemsetAsync(sg.disc_px, 0, 8 * (size_t)nblk, s));
-    }
-    CK(cudaMemsetAsync(ctx->seg_cls.p, 0, kSegBufBytes, s));
     CK(launch_seg_norm(da, sg, bt, ctx->num_sms, tu.blocks_per_sm, s));
-    CK(cudaEventRecord(ctx->evp1, s));
+    if (timed) CK(cudaEventRecord(ctx->evp1, s));
     CK(launch_seg_sort(da, sg, ctx->num_sms, s));
-    // the per-octave histograms plan the segments
-    long long *hc = ctx->h_seg + 4;
-    CK(cudaMemcpyAsync(hc, ctx->seg_cls.p, kSegClsBytes + kSegClsPxBytes, cudaMemcpyDeviceToHost, s));
-    CK(cudaStreamSynchronize(s));
-    const int *cls_items = (const int *)hc;
-    const int *cls_end = cls_items + kClasses;
-    const long long *cls_px = (const long long *)((const char *)hc + kSegClsBytes);
-    const long long budget = std::max<long long>(1, (long long)ctx->g.npix * kDepPerPix);
-    std::vector<SegSpan> spans;
-    plan_segments(cls_items, cls_end, cls_px, budget, spans);
-    for (size_t k = 0; k < spans.size(); ++k)
-        CK(launch_seg_deposit(da, sg, spans[k], (int)k, bt, ctx->num_sms, tu.blocks_per_sm, ctx->g.npix, s));
-    CK(cudaEventRecord(ctx->evdm, s));
+    CK(launch_seg_deposits(da, sg, bt, ctx->num_sms, tu.blocks_per_sm, ctx->g.npix, s));
+    DiscArgs db = da;
+    db.block_skip = sg.ctl;
+    CK(launch_disc_comp_block(db, ctx->num_sms, tu.blocks_per_sm, tu.block_threads, s));
+    if (timed) CK(cudaEventRecord(ctx->evdm, s));
     CK(launch_disc_comp_warp(da, ctx->num_sms, s));
-    ctx->seg_timed = true;
-    // prep, scan, scatter, item fill, pass 1, item sort (3), segments x
-    // (deposits, flush), warp class
-    ctx->launches += 9 + 2 * (long long)spans.size();
+    if (timed) ctx->seg_timed = true;
+    // prep, scan, scatter, headers, item count, mode, item fill, pass 1,
+    // octave histogram, scan, sort, plan, kSegSlots x (deposits, flush),
+    // per-disc block kernel, warp class
+    ctx->launches += 14 + 2 * kSegSlots;
     used = true;
     return DMANN_OK;
 }
@@ -957,6 +914,20 @@ namespace {
 // zero the planes, prep, key scan, queue scatter, disc kernels, finalize.
 // The workspace and the ring table must already exist: nothing here
 // allocates or synchronises, so the sequence can be captured in a graph.
+// Adds one observer's counters into the batch's sums (ctx->bstats: kept,
+// invalid, single, disc, block-class, deposits, then the kept flux).
+__global__ void k_batch_stats(const long long *ctr, const double *fsum, long long *out) {
+    out[0] += ctr[C_KEPT];
+    out[1] += ctr[C_INVALID];
+    out[2] += ctr[C_SINGLE];
+    out[3] += ctr[C_DISC];
+    out[4] += ctr[C_DISC_BLOCK];
+    out[5] += ctr[C_DEPOSITS];
+    reinterpret_cast<double *>(out)[6] += *fsum;
+}
+
+constexpr int kBatchStats = 7;
+
 dmann_status issue_observer(dmann_ctx *ctx, const float *const dev[6], int n, int nside,
                             const RingTables &rt, int precision, double *dmap) {
     cudaStream_t s = ctx->stream;
@@ -1002,11 +973,20 @@ dmann_status issue_observer(dmann_ctx *ctx, const float *const dev[6], int n, in
         da.queue = (const int *)ctx->queue.p;
         da.ctr = pa.ctr;
         da.acc = acc;
-        if (precision == DMANN_COMP_F32) da.chdr = headers_for(ctx, (size_t)n);
-        if (precision == DMANN_PLAIN_F64) CK(launch_disc_plain(da, ctx->num_sms, tu.blocks_per_sm, s, nullptr));
-        else CK(launch_disc_comp(da, ctx->num_sms, tu.blocks_per_sm, tu.block_threads, s, nullptr));
+        if (precision == DMANN_PLAIN_F64) {
+            CK(launch_disc_plain(da, ctx->num_sms, tu.blocks_per_sm, s, nullptr));
+        } else {
+            da.chdr = headers_for(ctx, (size_t)n);
+            bool seg = false;
+            dmann_status st = render_segmented(ctx, da, tu, (size_t)n, seg, false);
+            if (st != DMANN_OK) return st;
+            if (!seg) CK(launch_disc_comp(da, ctx->num_sms, tu.blocks_per_sm, tu.block_threads, s, nullptr));
+        }
     }
     CK(launch_finalize(acc, precision, ctx->g.npix, ctx->g.dOmega, scale, dmap, 0, s));
+    k_batch_stats<<<1, 1, 0, s>>>((const long long *)ctx->ctr.p, (const double *)ctx->fsum.p,
+                                  (long long *)ctx->bstats.p);
+    CK(cudaGetLastError());
     return DMANN_OK;
 }
 
@@ -1049,7 +1029,15 @@ dmann_status dmann_render_batch(dmann_ctx *ctx, const float *x, const float *y, 
         (st = ensure(ctx, ctx->ctr, 8 * C_COUNT)) || (st = ensure(ctx, ctx->fsum, 8)) ||
         (st = ensure(ctx, ctx->acc, 8 * Pmax)) || (st = ensure(ctx, ctx->map, 8 * Pmax)))
         return st;
-    if (precision == DMANN_COMP_F32) reserve_headers(ctx, n1);   // before any capture
+    if ((st = ensure(ctx, ctx->bstats, 8 * kBatchStats)) != DMANN_OK) return st;
+    // before any capture: the disc headers and the segmented render's buffers
+    // (the render checks them again and allocates nothing when they fit)
+    ctx->seg_plane = false;
+    if (precision == DMANN_COMP_F32) {
+        reserve_headers(ctx, n1);
+        ctx->seg_plane = ensure_opt(ctx->plane32, 4 * Pmax) && reserve_seg(ctx, N);
+        if (ctx->seg_plane) CK(cudaMemsetAsync(ctx->plane32.p, 0, 4 * Pmax, s));
+    }
     std::vector<RingTables> rts(n_obs);
     for (int k = 0; k < n_obs; k++)
         if ((st = ring_tables(ctx, nside[k], rts[k])) != DMANN_OK) return st;
@@ -1073,61 +1061,134 @@ dmann_status dmann_render_batch(dmann_ctx *ctx, const float *x, const float *y, 
     std::vector<char> on_dev(n_obs);
     bool all_dev = true;
     for (int k = 0; k < n_obs; k++) all_dev &= (on_dev[k] = is_device_ptr(maps[k])) != 0;
+    // the parameters a captured graph depends on: a batch that repeats them
+    // relaunches the cached graph instead of capturing again
+    std::vector<char> key;
+    auto put = [&key](const void *p, size_t nb) {
+        key.insert(key.end(), (const char *)p, (const char *)p + nb);
+    };
+    const unsigned long long gen = g_alloc_gen.load();
+    put(&gen, sizeof gen);
+    put(&n, sizeof n);
+    put(&n_obs, sizeof n_obs);
+    put(&precision, sizeof precision);
+    put(dev, sizeof dev);
+    put(nside, sizeof(int) * n_obs);
+    put(rot, sizeof(double) * 9 * n_obs);
+    put(opos, sizeof(double) * 3 * n_obs);
+    put(maps, sizeof(double *) * n_obs);
+    put(&ctx->unit_factor, sizeof ctx->unit_factor);
+    put(&ctx->hires, sizeof ctx->hires);
+    put(&ctx->flux_model, sizeof ctx->flux_model);
+    put(&ctx->vel_to_cgs, sizeof ctx->vel_to_cgs);
+    put(ctx->fcpos, sizeof ctx->fcpos);
+    put(&ctx->seg_plane, sizeof ctx->seg_plane);
+    for (int k = 0; k < n_obs; k++) put(&tuning_for(ctx, nside[k]), sizeof(dmann_tuning));
     double rot0[9], opos0[3];
     std::memcpy(rot0, ctx->rot, sizeof rot0);
     std::memcpy(opos0, ctx->opos, sizeof opos0);
     const bool had_frame = ctx->have_frame, had_geom = ctx->have_geom;
-    // device maps: the whole batch is captured into one CUDA graph and
-    // launched once; host maps go through the context's staging map.  The
-    // capture runs on the context's own stream (a caller's stream may be the
-    // legacy default stream, which cannot be captured), fenced to the
-    // caller's stream with events on both sides.
-    cudaGraph_t graph = nullptr;
-    cudaGraphExec_t exec = nullptr;
+    // device maps: the whole batch is captured into one CUDA graph (kept and
+    // relaunched while the batch's parameters repeat); host maps go through
+    // the context's staging map.  The graph runs on the context's own stream
+    // (a caller's stream may be the legacy default stream, which cannot be
+    // captured), fenced to the caller's stream with events on both sides.
     const cudaStream_t caller = s;
+    const long long launches0 = ctx->launches;
+    ctx->launches = 0;
     if (all_dev) {
         if (s != ctx->own) {
             CK(cudaEventRecord(ctx->evdm, s));
             CK(cudaStreamWaitEvent(ctx->own, ctx->evdm, 0));
         }
         s = ctx->own;
-        ctx->stream = s;
-        CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
     }
-    for (int k = 0; k < n_obs && st == DMANN_OK; k++) {
-        std::memcpy(ctx->rot, rot + 9 * k, sizeof(double) * 9);
-        std::memcpy(ctx->opos, opos + 3 * k, sizeof(double) * 3);
-        double *dmap = on_dev[k] ? maps[k] : (double *)ctx->map.p;
-        st = issue_observer(ctx, dev, (int)N, nside[k], rts[k], precision, dmap);
-        if (st == DMANN_OK && !on_dev[k]) {
-            const size_t P = 12 * (size_t)nside[k] * (size_t)nside[k];
-            cudaError_t e = cudaMemcpyAsync(maps[k], dmap, 8 * P, cudaMemcpyDeviceToHost, s);
-            if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-            if (e != cudaSuccess) st = fail(ctx, DMANN_ERR_CUDA, std::string("batch copy: ") + cudaGetErrorString(e));
+    const bool cached = all_dev && ctx->batch_exec && key == ctx->batch_key;
+    cudaGraph_t graph = nullptr;
+    if (!cached) {
+        if (all_dev) {
+            ctx->stream = s;
+            CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
         }
-    }
-    std::memcpy(ctx->rot, rot0, sizeof rot0);
-    std::memcpy(ctx->opos, opos0, sizeof opos0);
-    ctx->have_frame = had_frame;
-    ctx->have_geom = had_geom;
-    if (all_dev) {
-        cudaError_t e = cudaStreamEndCapture(s, &graph);
-        ctx->stream = caller;
-        if (st != DMANN_OK) {
-            if (graph) cudaGraphDestroy(graph);
-            return st;
+        cudaError_t e = cudaMemsetAsync(ctx->bstats.p, 0, 8 * kBatchStats, s);
+        if (e != cudaSuccess) st = fail(ctx, DMANN_ERR_CUDA, std::string("batch: ") + cudaGetErrorString(e));
+        for (int k = 0; k < n_obs && st == DMANN_OK; k++) {
+            std::memcpy(ctx->rot, rot + 9 * k, sizeof(double) * 9);
+            std::memcpy(ctx->opos, opos + 3 * k, sizeof(double) * 3);
+            double *dmap = on_dev[k] ? maps[k] : (double *)ctx->map.p;
+            st = issue_observer(ctx, dev, (int)N, nside[k], rts[k], precision, dmap);
+            if (st == DMANN_OK && !on_dev[k]) {
+                const size_t P = 12 * (size_t)nside[k] * (size_t)nside[k];
+                e = cudaMemcpyAsync(maps[k], dmap, 8 * P, cudaMemcpyDeviceToHost, s);
+                if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+                if (e != cudaSuccess) st = fail(ctx, DMANN_ERR_CUDA, std::string("batch copy: ") + cudaGetErrorString(e));
+            }
         }
-        if (e != cudaSuccess) return fail(ctx, DMANN_ERR_CUDA, std::string("batch capture: ") + cudaGetErrorString(e));
-        e = cudaGraphInstantiate(&exec, graph, 0);
-        if (e == cudaSuccess) e = cudaGraphLaunch(exec, s);
-        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-        if (exec) cudaGraphExecDestroy(exec);
-        cudaGraphDestroy(graph);
-        if (e != cudaSuccess) return fail(ctx, DMANN_ERR_CUDA, std::string("batch graph: ") + cudaGetErrorString(e));
+        std::memcpy(ctx->rot, rot0, sizeof rot0);
+        std::memcpy(ctx->opos, opos0, sizeof opos0);
+        ctx->have_frame = had_frame;
+        ctx->have_geom = had_geom;
+        if (all_dev) {
+            e = cudaStreamEndCapture(s, &graph);
+            ctx->stream = caller;
+            if (st != DMANN_OK) {
+                if (graph) cudaGraphDestroy(graph);
+                ctx->launches = launches0;
+                return st;
+            }
+            if (e != cudaSuccess) return fail(ctx, DMANN_ERR_CUDA, std::string("batch capture: ") + cudaGetErrorString(e));
+            // same topology (new frames, maps or units): update the kept
+            // graph in place; else instantiate afresh
+            bool updated = false;
+            if (ctx->batch_exec) {
+                cudaGraphExecUpdateResultInfo info;
+                updated = cudaGraphExecUpdate(ctx->batch_exec, graph, &info) == cudaSuccess;
+                if (!updated) {
+                    cudaGetLastError();
+                    cudaGraphExecDestroy(ctx->batch_exec);
+                    ctx->batch_exec = nullptr;
+                }
+            }
+            if (!updated) e = cudaGraphInstantiate(&ctx->batch_exec, graph, 0);
+            cudaGraphDestroy(graph);
+            ctx->batch_key.clear();
+            if (e != cudaSuccess) {
+                ctx->batch_exec = nullptr;
+                return fail(ctx, DMANN_ERR_CUDA, std::string("batch graph: ") + cudaGetErrorString(e));
+            }
+            ctx->batch_key = key;
+            ctx->batch_launches = ctx->launches;
+        }
     }
     if (st != DMANN_OK) return st;
+    if (all_dev) {
+        cudaError_t e = cudaEventRecord(ctx->ev0, s);
+        if (e == cudaSuccess) e = cudaGraphLaunch(ctx->batch_exec, s);
+        if (e == cudaSuccess) e = cudaEventRecord(ctx->ev1, s);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) return fail(ctx, DMANN_ERR_CUDA, std::string("batch graph: ") + cudaGetErrorString(e));
+        ctx->launches = ctx->batch_launches;
+    } else {
+        CK(cudaStreamSynchronize(s));
+    }
+    // the batch's counters: summed over its observers
+    long long hb[kBatchStats];
+    CK(cudaMemcpy(hb, ctx->bstats.p, sizeof hb, cudaMemcpyDeviceToHost));
     ctx->stats = dmann_stats{};
-    ctx->stats.n_in = n;
+    ctx->stats.n_in = n * n_obs;
+    ctx->stats.n_kept = hb[0];
+    ctx->stats.n_invalid = hb[1];
+    ctx->stats.n_single = hb[2];
+    ctx->stats.n_disc = hb[3];
+    ctx->stats.n_disc_block = hb[4];
+    ctx->stats.deposits = hb[5];
+    std::memcpy(&ctx->stats.total_flux, &hb[6], sizeof(double));
+    if (all_dev) {
+        float ms = 0.0f;
+        CK(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
+        ctx->stats.kernel_ms = ms;
+    }
+    ctx->stats.launches = ctx->launches;
     return DMANN_OK;
 }
 

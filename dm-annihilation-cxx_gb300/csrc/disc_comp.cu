@@ -136,9 +136,11 @@ constexpr int kWPB = 8, kRCHW = 64;    // warp kernel
 // discs first, claimed dynamically).  Block shapes: BT threads, runs of RCH
 // rings staged per chunk, MINB resident blocks per SM -- every shape fills
 // the SM with 2048 threads (fewer, with more registers each, measured slower)
-// and about 200 KB of staged runs.  The autotuner picks the shape.
+// and about 200 KB of staged runs.  The autotuner picks the shape.  Returns
+// at once when the segmented render took the block class (*a.block_skip).
 template <int BT, int RCH, int MINB>
 __global__ void __launch_bounds__(BT, MINB) k_comp_block(DiscArgs a) {
+    if (a.block_skip && *a.block_skip) return;
     __shared__ CompSmem<RCH> sm;
     __shared__ int s_q;
     const long long nblk = a.ctr[C_ADD_BLOCK];
@@ -370,6 +372,13 @@ cudaError_t launch_disc_comp_warp(const DiscArgs &a, int num_sms, cudaStream_t s
 }
 
 size_t comp_hdr_bytes() { return sizeof(CompHdr); }
+
+cudaError_t launch_disc_comp_block(const DiscArgs &a, int num_sms, int blocks_per_sm, int block_threads,
+                                   cudaStream_t s) {
+    if (block_threads == 128) return launch_block<128, 192, 16>(a, num_sms, blocks_per_sm, s);
+    if (block_threads == 512) return launch_block<512, 640, 4>(a, num_sms, blocks_per_sm, s);
+    return launch_block<256, 384, 8>(a, num_sms, blocks_per_sm, s);
+}
 
 cudaError_t launch_disc_comp(const DiscArgs &a, int num_sms, int blocks_per_sm, int block_threads,
                              cudaStream_t s, cudaEvent_t mid, bool headers) {

@@ -32,10 +32,10 @@
 // rounding (both take A and B rounded once to FP32).  Other discs take the
 // general per-pixel path of comp_engine.cuh (weight2 with run-time tiers).
 //
-// Normalisation sums.  Each lane sums its pixels of a run in plain FP32 (a
-// few weights) and adds that run partial into a two-float (s, c) with
-// Knuth's TwoSum, so every rounding of the additions across runs is kept;
-// the item's lanes are reduced as two-floats.
+// Normalisation sums.  Each lane sums at most kFoldPairs pixel pairs of a
+// run in plain FP32 and adds that partial into a two-float (s, c) with
+// Knuth's TwoSum, so every rounding of the additions across partials is
+// kept; the item's lanes are reduced as two-floats.
 //
 // Deposits and segments.  A deposit w (F + Flo) is rounded once to FP32 and
 // added with red.global.add.f32 into an FP32 plane: half the L2 reduction
@@ -54,9 +54,13 @@
 //   * Length.  A segment holds about kDepPerPix deposits per pixel (an
 //     octave with more is dealt round robin into several segments), so a
 //     pixel's FP32 partial sums stay short and their rounding errors random.
-// The host plans the segments from the per-octave histograms (plan_segments).
+// The plan is made on the device from the per-octave histograms
+// (k_seg_plan), and every kernel of the sequence reads the chunk's mode
+// (k_seg_decide) and returns at once when it has nothing to do, so the
+// whole render is one stream of launches with no host synchronisation.
 // Chunks too small for the L2 reduction rate to matter (a tunable threshold
-// on the estimated deposits) take the per-disc kernels with FP64 deposits.
+// on the estimated deposits), or with more work items than the item buffers
+// hold, take the per-disc kernels with FP64 deposits instead.
 #include "comp_engine.cuh"
 
 namespace dmann {
@@ -185,7 +189,7 @@ __device__ __forceinline__ float2 seg_weight2(const Ext &e, const SRun &r, float
 // each claim.
 template <int RCH, int S, class Body, class Done>
 __device__ inline void seg_walk(SegSmem<RCH> &sm, int n, Body body, Done ring_done) {
-    static_assert(S == 8 || S == 16 || S == 32, "lanes per ring");
+    static_assert(S == 4 || S == 8 || S == 16 || S == 32, "lanes per ring");
     constexpr int G = 32 / S;
     const int lane = threadIdx.x & 31, sl = lane % S;
     int q0 = 0;
@@ -209,11 +213,42 @@ __device__ inline void seg_walk(SegSmem<RCH> &sm, int n, Body body, Done ring_do
 }
 
 constexpr int kNormLanes = 8;    // lanes per ring in pass 1 (weights only)
-constexpr int kDepLanes = 16;    // lanes per ring in pass 2 (16 floats of the map per reduction)
+constexpr int kFoldPairs = 8;    // pass 1: pixel pairs per plain FP32 partial
+
+// Pass 2's walk: warps claim rings one at a time, and lane l takes the
+// pixel pairs l, l + 32, ... of each run, a pair being two map pixels
+// (2p, 2p + 1) -- 8-byte aligned, so one red.global.add.v2.f32 deposits
+// both, and a warp's reduction covers 64 contiguous floats.  body(run, j,
+// lo, hi) gets the run-local index j of the pair's first pixel and whether
+// that pixel (lo) and the next (hi) are in the run (a run's first and last
+// pair may hold one pixel of it).
+template <int RCH, class Body>
+__device__ inline void seg_walk_pairs(SegSmem<RCH> &sm, int n, Body body) {
+    const int lane = threadIdx.x & 31;
+    int q = 0;
+    if (lane == 0) q = atomicAdd(&sm.next_run, 1);
+    q = __shfl_sync(0xffffffffu, q, 0);
+    while (q < n) {
+        int qn = 0;
+        if (lane == 0) qn = atomicAdd(&sm.next_run, 1);
+#pragma unroll 1
+        for (int k = 0; k < 2; k++) {
+            if (k == 1 && !sm.run[2 * q].more) break;
+            const SRun r = sm.run[2 * q + k];
+            const int p0 = r.pix0 >> 1, np = ((r.pix0 + r.cnt - 1) >> 1) - p0 + 1;
+            for (int pp = lane; pp < np; pp += 32) {
+                const int j = 2 * (p0 + pp) - r.pix0;
+                body(r, j, j >= 0, j + 1 < r.cnt);
+            }
+        }
+        q = __shfl_sync(0xffffffffu, qn, 0);
+    }
+}
 
 // Claims the next work item for the block (thread 0: first + t stride for
 // the t-th claim, below end) and stages its disc's header; false when the
-// item range is exhausted.
+// item range is exhausted.  Callers return at once unless the chunk is
+// segmented (sg.ctl[0]), so the item counts are within the buffers.
 template <int BT, int RCH>
 __device__ inline bool seg_claim(const DiscArgs &a, const SegArgs &sg, const int2 *items,
                                  SegSmem<RCH> &sm, unsigned long long *next, long long stride,
@@ -221,7 +256,7 @@ __device__ inline bool seg_claim(const DiscArgs &a, const SegArgs &sg, const int
     if (threadIdx.x == 0) {
         const long long t = (long long)atomicAdd(next, 1ull);
         const long long k = first + t * stride;
-        sm.item = k < min(end, sg.n_items) ? (int)k : -1;
+        sm.item = k < end ? (int)k : -1;
     }
     __syncthreads();
     const int k = sm.item;
@@ -249,8 +284,16 @@ __device__ inline void norm_item(const DiscArgs &a, SegSmem<RCH> &sm, int r0, in
                                  float &S_lo, int &total) {
     const Ext e = sm.h.ext;
     total = seg_build<BT, RCH>(a, sm, r0, n, POLY);
-    float s = 0.0f, c = 0.0f;   // this lane's two-float sum of its run partials
-    float2 part = f2(0.0f);
+    float s = 0.0f, c = 0.0f;   // this lane's two-float sum of its partials
+    float2 part = f2(0.0f);     // plain FP32 partial of at most kFoldPairs pixel pairs
+    int np = 0;
+    auto fold = [&]() {
+        float err;
+        s = two_sum(s, part.x + part.y, err);
+        c += err;
+        part = f2(0.0f);
+        np = 0;
+    };
     seg_walk<RCH, kNormLanes>(
         sm, n,
         [&](const SRun &r, int j, bool second) {
@@ -258,13 +301,9 @@ __device__ inline void norm_item(const DiscArgs &a, SegSmem<RCH> &sm, int r0, in
             float2 w = seg_weight2<POLY>(e, r, make_float2(jf, jf + (float)kNormLanes));
             if (!second) w.y = 0.0f;
             part = add2(part, w);
+            if (++np == kFoldPairs) fold();   // long rings: keep the plain partials short
         },
-        [&]() {
-            float err;
-            s = two_sum(s, part.x + part.y, err);
-            c += err;
-            part = f2(0.0f);
-        });
+        fold);
     warp_sum_ff(s, c);
     if ((threadIdx.x & 31) == 0) sm.red2[threadIdx.x >> 5] = make_float2(s, c);
     __syncthreads();
@@ -279,10 +318,12 @@ __device__ inline void norm_item(const DiscArgs &a, SegSmem<RCH> &sm, int r0, in
 
 template <int BT, int RCH, int MINB>
 __global__ void __launch_bounds__(BT, MINB) k_seg_norm(DiscArgs a, SegArgs sg) {
+    if (sg.ctl[0] == 0) return;
     __shared__ SegSmem<RCH> sm;
     int2 it;
+    const long long n_items = a.ctr[C_SEG_ITEMS];
     while (seg_claim<BT, RCH>(a, sg, sg.items, sm, (unsigned long long *)(a.ctr + C_SEG_NEXT_NORM), 1, 0,
-                              sg.n_items, it)) {
+                              n_items, it)) {
         int r0, n;
         item_rings(sm.h, it.y, r0, n);
         const bool poly = sm.h.ext.tier_x < 2 && sm.h.ext.tier_h < 2;
@@ -304,24 +345,25 @@ __device__ inline void dep_item(const DiscArgs &a, SegSmem<RCH> &sm, int r0, int
                                 float *plane) {
     const Ext e = sm.h.ext;
     seg_build<BT, RCH>(a, sm, r0, n, POLY);
-    seg_walk<RCH, kDepLanes>(
-        sm, n,
-        [&](const SRun &r, int j, bool second) {
-            const float jf = (float)j;
-            const float2 w = seg_weight2<POLY>(e, r, make_float2(jf, jf + (float)kDepLanes));
-            const float2 p = fma2(w, f2(F), mul2(w, f2(Flo)));   // w (F + Flo), rounded once
-            float *const m = plane + (r.pix0 + j);
-            red_add_f32(m, p.x);
-            if (second) red_add_f32(m + kDepLanes, p.y);
-        },
-        []() {});
+    seg_walk_pairs<RCH>(sm, n, [&](const SRun &r, int j, bool lo, bool hi) {
+        const float jf = (float)j;
+        const float2 w = seg_weight2<POLY>(e, r, make_float2(jf, jf + 1.0f));
+        const float2 p = fma2(w, f2(F), mul2(w, f2(Flo)));   // w (F + Flo), rounded once
+        float *const m = plane + (r.pix0 + j);
+        if (lo && hi) red_add_v2_f32(m, p.x, p.y);
+        else if (lo) red_add_f32(m, p.x);
+        else red_add_f32(m + 1, p.y);
+    });
     __syncthreads();
 }
 
-// One segment of deposits (its items of the sorted list, see SegSpan).
+// Segment seg of the plan: its items of the sorted list (see SegSpan);
+// returns at once when the plan has fewer segments.
 template <int BT, int RCH, int MINB>
-__global__ void __launch_bounds__(BT, MINB) k_seg_dep(DiscArgs a, SegArgs sg, SegSpan sp, int seg) {
+__global__ void __launch_bounds__(BT, MINB) k_seg_dep(DiscArgs a, SegArgs sg, int seg) {
+    if (sg.ctl[0] == 0 || seg >= sg.ctl[1]) return;
     __shared__ SegSmem<RCH> sm;
+    const SegSpan sp = sg.spans[seg];
     int2 it;
     while (seg_claim<BT, RCH>(a, sg, sg.sorted, sm, sg.seg_next + seg, sp.stride, sp.lo + sp.offset,
                               sp.hi, it)) {
@@ -352,7 +394,7 @@ __global__ void __launch_bounds__(BT, MINB) k_seg_dep(DiscArgs a, SegArgs sg, Se
 
 // Items of each block-class disc: ring chunking from the cap-area estimate,
 // the item count and its first item (claimed from C_SEG_ITEMS), and the
-// estimated deposits (for the segment count).
+// estimated deposits (for the chunk's mode); clears the disc's pass-1 sums.
 template <int RCH>
 __global__ void __launch_bounds__(256) k_seg_count(DiscArgs a, SegArgs sg) {
     const long long nblk = a.ctr[C_ADD_BLOCK];
@@ -370,6 +412,8 @@ __global__ void __launch_bounds__(256) k_seg_count(DiscArgs a, SegArgs sg) {
         sg.disc_first[q] = (long long)atomicAdd((unsigned long long *)(a.ctr + C_SEG_ITEMS),
                                                 (unsigned long long)nit);
         sg.disc_nitems[q] = nit;
+        sg.disc_S[q] = 0.0;
+        sg.disc_px[q] = 0;
         est_sum += (long long)est;
     }
     est_sum = warp_sum_ll(est_sum);
@@ -377,14 +421,23 @@ __global__ void __launch_bounds__(256) k_seg_count(DiscArgs a, SegArgs sg) {
         atomicAdd((unsigned long long *)(a.ctr + C_SEG_EST), (unsigned long long)est_sum);
 }
 
+// The chunk's mode: segmented when its estimated deposits reach min_est and
+// its items fit the item buffers (else the per-disc kernels deposit in FP64).
+__global__ void k_seg_decide(DiscArgs a, SegArgs sg) {
+    const long long items = a.ctr[C_SEG_ITEMS], est = a.ctr[C_SEG_EST];
+    const int mode = (items > 0 && items <= sg.cap && est >= sg.min_est) ? 1 : 0;
+    sg.ctl[0] = mode;
+    a.ctr[C_SEG_MODE] = mode;
+}
+
 __global__ void __launch_bounds__(256) k_seg_fill(DiscArgs a, SegArgs sg) {
+    if (sg.ctl[0] == 0) return;
     const long long nblk = a.ctr[C_ADD_BLOCK];
     const long long stride = (long long)gridDim.x * blockDim.x;
     for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < nblk; q += stride) {
         const long long f = sg.disc_first[q];
         const int nit = sg.disc_nitems[q];
-        for (int i = 0; i < nit; i++)
-            if (f + i < sg.n_items) sg.items[f + i] = make_int2((int)q, i);
+        for (int i = 0; i < nit; i++) sg.items[f + i] = make_int2((int)q, i);
     }
 }
 
@@ -400,6 +453,7 @@ __device__ inline int seg_class(const DiscArgs &a, const SegArgs &sg, long long 
 
 // Items and pixels per class (sg.cls[0 .. kClasses), sg.cls_px).
 __global__ void __launch_bounds__(256) k_seg_class(DiscArgs a, SegArgs sg) {
+    if (sg.ctl[0] == 0) return;
     __shared__ int hist[kClasses];
     __shared__ unsigned long long px[kClasses];
     for (int i = threadIdx.x; i < kClasses; i += blockDim.x) {
@@ -424,6 +478,7 @@ __global__ void __launch_bounds__(256) k_seg_class(DiscArgs a, SegArgs sg) {
 // Exclusive scan of the class histogram into the classes' first slots
 // (sg.cls[kClasses .. 2 kClasses)); one block of kClasses threads.
 __global__ void __launch_bounds__(kClasses) k_seg_cscan(SegArgs sg) {
+    if (sg.ctl[0] == 0) return;
     int total;
     const int v = sg.cls[threadIdx.x];
     const int ex = warp_excl_scan(v, total);
@@ -437,18 +492,73 @@ __global__ void __launch_bounds__(kClasses) k_seg_cscan(SegArgs sg) {
 
 // Each disc's items into its class's range of the sorted list.
 __global__ void __launch_bounds__(256) k_seg_sort(DiscArgs a, SegArgs sg) {
+    if (sg.ctl[0] == 0) return;
     const long long nblk = a.ctr[C_ADD_BLOCK];
     const long long stride = (long long)gridDim.x * blockDim.x;
     for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < nblk; q += stride) {
         const int nit = sg.disc_nitems[q];
         const long long f = atomicAdd(sg.cls + kClasses + seg_class(a, sg, q), nit);
-        for (int i = 0; i < nit; i++)
-            if (f + i < sg.n_items) sg.sorted[f + i] = make_int2((int)q, i);
+        for (int i = 0; i < nit; i++) sg.sorted[f + i] = make_int2((int)q, i);
     }
 }
 
-// acc64 += plane, plane = 0 (four pixels per thread; npix is a multiple of 4).
-__global__ void __launch_bounds__(256) k_seg_flush(float *plane, double *acc, long long npix4) {
+// The segment plan from the per-octave histograms (one thread): n[c] items
+// ending at slot end[c] of the sorted list (k_seg_sort leaves each octave's
+// end slot), px[c] deposits.  Consecutive octaves are grouped while the
+// group spans at most kClassSpan octaves and budget deposits; an octave with
+// more than budget deposits is dealt round robin into ceil(px / budget)
+// segments of its own.  Class 0 (discs with no weighted deposits: single
+// pixels, zero flux) is one segment.  At most kSegSlots segments: the budget
+// doubles until the plan fits.
+__global__ void k_seg_plan(SegArgs sg) {
+    if (sg.ctl[0] == 0) return;
+    const int *n = sg.cls, *end = sg.cls + kClasses;
+    const long long *px = sg.cls_px;
+    for (long long budget = max(1LL, sg.budget);; budget *= 2) {
+        int ns = 0;
+        auto push = [&](long long lo, long long hi, int stride, int offset) {
+            if (ns < kSegSlots) sg.spans[ns] = SegSpan{lo, hi, stride, offset};
+            ns++;
+        };
+        if (n[0] > 0) push((long long)end[0] - n[0], end[0], 1, 0);
+        int c0 = -1;
+        long long lo = 0, hi = 0, acc = 0;
+        for (int c = 1; c < kClasses; ++c) {
+            if (n[c] == 0) continue;
+            const long long f = (long long)end[c] - n[c];
+            if (px[c] > budget) {
+                if (c0 >= 0) push(lo, hi, 1, 0);
+                c0 = -1;
+                acc = 0;
+                const long long m = min((long long)n[c], (px[c] + budget - 1) / budget);
+                for (long long k = 0; k < m; ++k) push(f, end[c], (int)m, (int)k);
+                continue;
+            }
+            if (c0 >= 0 && (c - c0 >= kClassSpan || acc + px[c] > budget)) {
+                push(lo, hi, 1, 0);
+                c0 = -1;
+                acc = 0;
+            }
+            if (c0 < 0) {
+                c0 = c;
+                lo = f;
+            }
+            hi = end[c];
+            acc += px[c];
+        }
+        if (c0 >= 0) push(lo, hi, 1, 0);
+        if (ns <= kSegSlots) {
+            sg.ctl[1] = ns;
+            return;
+        }
+    }
+}
+
+// After segment seg: acc64 += plane, plane = 0 (four pixels per thread;
+// npix is a multiple of 4); returns at once when the plan has no segment seg.
+__global__ void __launch_bounds__(256) k_seg_flush(const int *ctl, int seg, float *plane, double *acc,
+                                                   long long npix4) {
+    if (ctl[0] == 0 || seg >= ctl[1]) return;
     const long long stride = (long long)gridDim.x * blockDim.x;
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < npix4; i += stride) {
         const float4 v = reinterpret_cast<float4 *>(plane)[i];
@@ -468,11 +578,14 @@ __global__ void __launch_bounds__(256) k_seg_flush(float *plane, double *acc, lo
 
 template <int BT, int RCH, int MINB>
 int grid_of(int num_sms, int blocks_per_sm) {
-    int occ = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_seg_norm<BT, RCH, MINB>, BT, 0) != cudaSuccess) {
-        cudaGetLastError();
-        occ = 1;
-    }
+    static const int occ = [] {
+        int o = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, k_seg_norm<BT, RCH, MINB>, BT, 0) != cudaSuccess) {
+            cudaGetLastError();
+            o = 1;
+        }
+        return o;
+    }();
     const int bps = blocks_per_sm > 0 ? min(blocks_per_sm, occ) : occ;
     return num_sms * (bps < 1 ? 1 : bps);
 }
@@ -487,13 +600,17 @@ cudaError_t launch_norm(const DiscArgs &a, const SegArgs &sg, int num_sms, int b
 }
 
 template <int BT, int RCH, int MINB>
-cudaError_t launch_deposit(const DiscArgs &a, const SegArgs &sg, const SegSpan &span, int seg, int num_sms,
-                           int blocks_per_sm, int npix, cudaStream_t s) {
-    k_seg_dep<BT, RCH, MINB><<<grid_of<BT, RCH, MINB>(num_sms, blocks_per_sm), BT, 0, s>>>(a, sg, span, seg);
-    cudaError_t e = cudaGetLastError();
-    if (e != cudaSuccess) return e;
-    k_seg_flush<<<num_sms * 8, 256, 0, s>>>(sg.plane, a.acc.acc64, npix / 4);
-    return cudaGetLastError();
+cudaError_t launch_deposits(const DiscArgs &a, const SegArgs &sg, int num_sms, int blocks_per_sm, int npix,
+                            cudaStream_t s) {
+    const int grid = grid_of<BT, RCH, MINB>(num_sms, blocks_per_sm);
+    for (int k = 0; k < kSegSlots; k++) {
+        k_seg_dep<BT, RCH, MINB><<<grid, BT, 0, s>>>(a, sg, k);
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+        k_seg_flush<<<num_sms * 8, 256, 0, s>>>(sg.ctl, k, sg.plane, a.acc.acc64, npix / 4);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    }
+    return cudaSuccess;
 }
 
 }  // namespace
@@ -502,6 +619,9 @@ cudaError_t launch_seg_count(const DiscArgs &a, const SegArgs &sg, int block_thr
                              cudaStream_t s) {
     if (block_threads == 256) k_seg_count<256><<<num_sms * 8, 256, 0, s>>>(a, sg);
     else k_seg_count<128><<<num_sms * 8, 256, 0, s>>>(a, sg);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    k_seg_decide<<<1, 1, 0, s>>>(a, sg);
     return cudaGetLastError();
 }
 
@@ -518,15 +638,15 @@ cudaError_t launch_seg_sort(const DiscArgs &a, const SegArgs &sg, int num_sms, c
     k_seg_cscan<<<1, kClasses, 0, s>>>(sg);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     k_seg_sort<<<num_sms * 8, 256, 0, s>>>(a, sg);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    k_seg_plan<<<1, 1, 0, s>>>(sg);
     return cudaGetLastError();
 }
 
-cudaError_t launch_seg_deposit(const DiscArgs &a, const SegArgs &sg, const SegSpan &span, int seg,
-                               int block_threads, int num_sms, int blocks_per_sm, int npix,
-                               cudaStream_t s) {
-    if (block_threads == 256)
-        return launch_deposit<256, 256, 8>(a, sg, span, seg, num_sms, blocks_per_sm, npix, s);
-    return launch_deposit<128, 128, 16>(a, sg, span, seg, num_sms, blocks_per_sm, npix, s);
+cudaError_t launch_seg_deposits(const DiscArgs &a, const SegArgs &sg, int block_threads, int num_sms,
+                                int blocks_per_sm, int npix, cudaStream_t s) {
+    if (block_threads == 256) return launch_deposits<256, 256, 8>(a, sg, num_sms, blocks_per_sm, npix, s);
+    return launch_deposits<128, 128, 16>(a, sg, num_sms, blocks_per_sm, npix, s);
 }
 
 }  // namespace dmann

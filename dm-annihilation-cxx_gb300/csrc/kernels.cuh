@@ -24,16 +24,21 @@ constexpr int kKeys = kBuckets * kCells;
 // Segmented render (disc_seg.cu).  The items are sorted into kClasses
 // octaves of their disc's deposit scale; a segment of deposits spans at most
 // kClassSpan consecutive octaves and about kDepPerPix FP32 additions per
-// pixel (kSegMax segments at most per chunk).  Chunks whose estimated
-// deposits are below 2^seg_min_deposits_log2 (a tunable) deposit in FP64.
+// pixel, with kSegSlots segments at most per chunk (the plan is made on the
+// device; each chunk launches kSegSlots deposit/flush pairs, the unused ones
+// return at once).  Chunks whose estimated deposits are below
+// 2^seg_min_deposits_log2 (a tunable), or whose work items exceed the item
+// buffers, deposit in FP64 with the per-disc kernels.
 constexpr int kClasses = 256;
 constexpr int kClassSpan = 2;
 constexpr int kDepPerPix = 512;
-constexpr int kSegMax = 1024;
-// The segment buffer (SegArgs.cls, cls_px, seg_next, in this order).
+constexpr int kSegSlots = 64;
+// The segment buffer, zeroed per chunk: cls, cls_px, seg_next, spans, ctl.
 constexpr size_t kSegClsBytes = 2 * 4 * kClasses;
 constexpr size_t kSegClsPxBytes = 8 * kClasses;
-constexpr size_t kSegBufBytes = kSegClsBytes + kSegClsPxBytes + 8 * kSegMax;
+constexpr size_t kSegNextBytes = 8 * kSegSlots;
+constexpr size_t kSegSpanBytes = 24 * kSegSlots;
+constexpr size_t kSegBufBytes = kSegClsBytes + kSegClsPxBytes + kSegNextBytes + kSegSpanBytes + 16;
 
 enum Ctr {
     C_KEPT = 0, C_SINGLE, C_DISC, C_DISC_BLOCK, C_DEPOSITS, C_INVALID,
@@ -41,6 +46,7 @@ enum Ctr {
     C_SEG_ITEMS,       // work items of the chunk's block-class discs
     C_SEG_EST,         // their estimated pixels (cap areas)
     C_SEG_NEXT_NORM,   // items claimed by pass 1
+    C_SEG_MODE,        // 1: the chunk took the segmented render
     C_COUNT
 };
 constexpr int kCtrChunkFirst = C_ADD_DISC;
@@ -107,21 +113,9 @@ struct DiscArgs {
     // compensated form: comp_hdr_bytes() per queue slot, filled by the disc
     // launch; null computes each header inside the disc kernels instead
     CompHdr *chdr = nullptr;
-};
-
-// Segmented render of the block-class discs (disc_seg.cu).
-struct SegArgs {
-    int2 *items;              // (queue slot, item index within its disc), queue order
-    int2 *sorted;             // the same items in ascending octave of the disc's F
-    int *cls;                 // [2 kClasses]: items per octave, then each octave's first slot
-    long long *cls_px;        // [kClasses]: pixels (deposits) per octave
-    unsigned long long *seg_next;   // [kSegMax]: items claimed by each segment
-    long long n_items;
-    long long *disc_first;    // per block-class disc: its first item
-    int *disc_nitems;         //   its item count
-    double *disc_S;           //   the sum of its weights (pass 1; zeroed by the caller)
-    long long *disc_px;       //   its pixel count (pass 1; zeroed by the caller)
-    float *plane;             // FP32 deposit plane, npix floats, zero between segments
+    // compensated block kernel: returns at once when *block_skip != 0 (the
+    // segmented render took the chunk's block class); null = never
+    const int *block_skip = nullptr;
 };
 
 // One segment of deposits: items lo + offset, lo + offset + stride, ... below
@@ -129,6 +123,26 @@ struct SegArgs {
 struct SegSpan {
     long long lo, hi;
     int stride, offset;
+};
+static_assert(sizeof(SegSpan) == 24, "the segment buffer holds 24-byte spans");
+
+// Segmented render of the block-class discs (disc_seg.cu).
+struct SegArgs {
+    int2 *items;              // (queue slot, item index within its disc), queue order
+    int2 *sorted;             // the same items in ascending octave of the disc's F
+    long long cap;            // capacity of items and sorted
+    int *cls;                 // [2 kClasses]: items per octave, then each octave's first slot
+    long long *cls_px;        // [kClasses]: pixels (deposits) per octave
+    unsigned long long *seg_next;   // [kSegSlots]: items claimed by each segment
+    SegSpan *spans;           // [kSegSlots]: the segment plan
+    int *ctl;                 // [0] mode (1 segmented, 0 per-disc kernels), [1] segments
+    long long min_est;        // estimated deposits from which the chunk is segmented
+    long long budget;         // deposits per segment before the plan splits an octave
+    long long *disc_first;    // per block-class disc: its first item
+    int *disc_nitems;         //   its item count
+    double *disc_S;           //   the sum of its weights (pass 1)
+    long long *disc_px;       //   its pixel count (pass 1)
+    float *plane;             // FP32 deposit plane, npix floats, zero between segments
 };
 
 // prep.cu
@@ -156,18 +170,22 @@ size_t comp_hdr_bytes();
 cudaError_t launch_hdr(const DiscArgs &a, int num_sms, cudaStream_t s);
 // the warp-per-particle compensated kernel alone (the warp class)
 cudaError_t launch_disc_comp_warp(const DiscArgs &a, int num_sms, cudaStream_t s);
-// disc_seg.cu: the item count of every block-class disc (needs the headers);
-// the item list and pass 1; the items sorted by octave (with the per-octave
-// histograms); one segment of deposits followed by its flush.
-// block_threads 128 or 256 picks the block shape.
+// disc_seg.cu, in stream order (nothing synchronises with the host, so
+// the sequence can be captured in a graph): the item count of every
+// block-class disc (needs the headers) and the chunk's mode; the item list
+// and pass 1; the items sorted by octave and the segment plan; the
+// kSegSlots deposit segments with their flushes.  block_threads 128 or 256
+// picks the block shape.
 cudaError_t launch_seg_count(const DiscArgs &a, const SegArgs &sg, int block_threads, int num_sms,
                              cudaStream_t s);
 cudaError_t launch_seg_norm(const DiscArgs &a, const SegArgs &sg, int block_threads, int num_sms,
                             int blocks_per_sm, cudaStream_t s);
 cudaError_t launch_seg_sort(const DiscArgs &a, const SegArgs &sg, int num_sms, cudaStream_t s);
-cudaError_t launch_seg_deposit(const DiscArgs &a, const SegArgs &sg, const SegSpan &span, int seg,
-                               int block_threads, int num_sms, int blocks_per_sm, int npix,
-                               cudaStream_t s);
+cudaError_t launch_seg_deposits(const DiscArgs &a, const SegArgs &sg, int block_threads, int num_sms,
+                                int blocks_per_sm, int npix, cudaStream_t s);
+// disc_comp.cu: the compensated block kernel alone (headers built)
+cudaError_t launch_disc_comp_block(const DiscArgs &a, int num_sms, int blocks_per_sm, int block_threads,
+                                   cudaStream_t s);
 // adjoint.cu: gradients of the plain-form map for dL/dmap = gmap; grad is
 // [6][n] (x, y, z, m, rho, h); oacc[12] (zeroed by the caller) receives
 // sum_i dL/du_i and dL/drot (row-major).  Needs the prep outputs (with cls)
