@@ -65,6 +65,10 @@ def test_batch_honours_per_nside_tuning(setup):
         par.set_observer(opos)
         frames.append((np.array(par.rot_flat()), opos))
         nsides.append(ns)
+    # the per-disc kernels' FP64 deposits (this halo's fat particles would
+    # take the segmented render, whose FP32 partial sums depend on the order
+    # of the deposits at their own ~1e-7 level)
+    r.set_tuning(seg_min_deposits_log2=62)
     base = r.render_batch(P.as_dict(), frames, nsides, COMP)
     r.set_tuning(nside=64, block_threads=128, warp_max_pixels=64)
     r.set_tuning(nside=128, block_threads=512, warp_max_pixels=8192)
@@ -73,6 +77,7 @@ def test_batch_honours_per_nside_tuning(setup):
                    COMP, outs=outs)
     r.clear_tuning(64)
     r.clear_tuning(128)
+    r.set_tuning(seg_min_deposits_log2=28)
     par.set_observer(P.obs_pos)
     for b, o in zip(base, outs):
         o = o.cpu().numpy()
