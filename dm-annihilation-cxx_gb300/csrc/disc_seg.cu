@@ -32,10 +32,11 @@
 // rounding (both take A and B rounded once to FP32).  Other discs take the
 // general per-pixel path of comp_engine.cuh (weight2 with run-time tiers).
 //
-// Normalisation sums.  Each lane sums at most kFoldPairs pixel pairs of a
-// run in plain FP32 and adds that partial into a two-float (s, c) with
-// Knuth's TwoSum, so every rounding of the additions across partials is
-// kept; the item's lanes are reduced as two-floats.
+// Normalisation sums.  Each lane sums its pixels of a ring in plain FP32
+// (at most kFoldPairs pixel pairs at a time for the large discs, whose
+// rings can hold the whole ring of the map) and adds that partial into a
+// two-float (s, c) with Knuth's TwoSum, so every rounding of the additions
+// across partials is kept; the item's lanes are reduced as two-floats.
 //
 // Deposits and segments.  A deposit w (F + Flo) is rounded once to FP32 and
 // added with red.global.add.f32 into an FP32 plane: half the L2 reduction
@@ -213,37 +214,9 @@ __device__ inline void seg_walk(SegSmem<RCH> &sm, int n, Body body, Done ring_do
 }
 
 constexpr int kNormLanes = 8;    // lanes per ring in pass 1 (weights only)
-constexpr int kFoldPairs = 8;    // pass 1: pixel pairs per plain FP32 partial
+constexpr int kDepLanes = 32;    // lanes per ring in pass 2 (a warp's reduction covers 32 floats)
+constexpr int kFoldPairs = 8;    // pass 1, large discs: pixel pairs per plain FP32 partial
 
-// Pass 2's walk: warps claim rings one at a time, and lane l takes the
-// pixel pairs l, l + 32, ... of each run, a pair being two map pixels
-// (2p, 2p + 1) -- 8-byte aligned, so one red.global.add.v2.f32 deposits
-// both, and a warp's reduction covers 64 contiguous floats.  body(run, j,
-// lo, hi) gets the run-local index j of the pair's first pixel and whether
-// that pixel (lo) and the next (hi) are in the run (a run's first and last
-// pair may hold one pixel of it).
-template <int RCH, class Body>
-__device__ inline void seg_walk_pairs(SegSmem<RCH> &sm, int n, Body body) {
-    const int lane = threadIdx.x & 31;
-    int q = 0;
-    if (lane == 0) q = atomicAdd(&sm.next_run, 1);
-    q = __shfl_sync(0xffffffffu, q, 0);
-    while (q < n) {
-        int qn = 0;
-        if (lane == 0) qn = atomicAdd(&sm.next_run, 1);
-#pragma unroll 1
-        for (int k = 0; k < 2; k++) {
-            if (k == 1 && !sm.run[2 * q].more) break;
-            const SRun r = sm.run[2 * q + k];
-            const int p0 = r.pix0 >> 1, np = ((r.pix0 + r.cnt - 1) >> 1) - p0 + 1;
-            for (int pp = lane; pp < np; pp += 32) {
-                const int j = 2 * (p0 + pp) - r.pix0;
-                body(r, j, j >= 0, j + 1 < r.cnt);
-            }
-        }
-        q = __shfl_sync(0xffffffffu, qn, 0);
-    }
-}
 
 // Claims the next work item for the block (thread 0: first + t stride for
 // the t-th claim, below end) and stages its disc's header; false when the
@@ -301,7 +274,10 @@ __device__ inline void norm_item(const DiscArgs &a, SegSmem<RCH> &sm, int r0, in
             float2 w = seg_weight2<POLY>(e, r, make_float2(jf, jf + (float)kNormLanes));
             if (!second) w.y = 0.0f;
             part = add2(part, w);
-            if (++np == kFoldPairs) fold();   // long rings: keep the plain partials short
+            // the large discs' rings are long (up to the whole ring): keep the
+            // plain partials short; the polynomial path's rings are short enough
+            if constexpr (!POLY)
+                if (++np == kFoldPairs) fold();
         },
         fold);
     warp_sum_ff(s, c);
@@ -345,15 +321,17 @@ __device__ inline void dep_item(const DiscArgs &a, SegSmem<RCH> &sm, int r0, int
                                 float *plane) {
     const Ext e = sm.h.ext;
     seg_build<BT, RCH>(a, sm, r0, n, POLY);
-    seg_walk_pairs<RCH>(sm, n, [&](const SRun &r, int j, bool lo, bool hi) {
-        const float jf = (float)j;
-        const float2 w = seg_weight2<POLY>(e, r, make_float2(jf, jf + 1.0f));
-        const float2 p = fma2(w, f2(F), mul2(w, f2(Flo)));   // w (F + Flo), rounded once
-        float *const m = plane + (r.pix0 + j);
-        if (lo && hi) red_add_v2_f32(m, p.x, p.y);
-        else if (lo) red_add_f32(m, p.x);
-        else red_add_f32(m + 1, p.y);
-    });
+    seg_walk<RCH, kDepLanes>(
+        sm, n,
+        [&](const SRun &r, int j, bool second) {
+            const float jf = (float)j;
+            const float2 w = seg_weight2<POLY>(e, r, make_float2(jf, jf + (float)kDepLanes));
+            const float2 p = fma2(w, f2(F), mul2(w, f2(Flo)));   // w (F + Flo), rounded once
+            float *const m = plane + (r.pix0 + j);
+            red_add_f32(m, p.x);
+            if (second) red_add_f32(m + kDepLanes, p.y);
+        },
+        []() {});
     __syncthreads();
 }
 
