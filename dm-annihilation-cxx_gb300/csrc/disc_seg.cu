@@ -214,8 +214,43 @@ __device__ inline void seg_walk(SegSmem<RCH> &sm, int n, Body body, Done ring_do
 }
 
 constexpr int kNormLanes = 8;    // lanes per ring in pass 1 (weights only)
-constexpr int kDepLanes = 32;    // lanes per ring in pass 2 (a warp's reduction covers 32 floats)
+constexpr int kDepLanes = 32;    // lanes per ring in pass 2's run walk
 constexpr int kFoldPairs = 8;    // pass 1, large discs: pixel pairs per plain FP32 partial
+constexpr bool kDepSectors = true;   // pass 2 walks 32-byte sectors (seg_walk_sectors)
+
+// Pass 2's sector walk: warps claim four rings at a time, eight lanes per
+// ring, and lane l of a group takes map pixel 8 m + l of every 32-byte
+// sector m the run touches (two sectors per step: pixels j and j + 8), so
+// each group's reduction instruction covers exactly one aligned sector --
+// the fewest L2 sectors per deposit a scalar FP32 reduction can reach --
+// while the per-ring work is shared by four rings as in pass 1.
+// body(run, j, in0, in1) gets the run-local index j of the lane's first
+// pixel (negative before the run) and whether j and j + 8 are in the run.
+template <int RCH, class Body>
+__device__ inline void seg_walk_sectors(SegSmem<RCH> &sm, int n, Body body) {
+    const int lane = threadIdx.x & 31, sl = lane & 7;
+    int q0 = 0;
+    if (lane == 0) q0 = atomicAdd(&sm.next_run, 4);
+    q0 = __shfl_sync(0xffffffffu, q0, 0);
+    while (q0 < n) {
+        int qn = 0;
+        if (lane == 0) qn = atomicAdd(&sm.next_run, 4);
+        const int q = q0 + (lane >> 3);
+        if (q < n) {
+#pragma unroll 1
+            for (int k = 0; k < 2; k++) {
+                if (k == 1 && !sm.run[2 * q].more) break;
+                const SRun r = sm.run[2 * q + k];
+                const int a0 = r.pix0 >> 3, ns = ((r.pix0 + r.cnt + 7) >> 3) - a0;
+                for (int t = 0; t < ns; t += 2) {
+                    const int j = ((a0 + t) << 3) + sl - r.pix0;
+                    body(r, j, (unsigned)j < (unsigned)r.cnt, (unsigned)(j + 8) < (unsigned)r.cnt);
+                }
+            }
+        }
+        q0 = __shfl_sync(0xffffffffu, qn, 0);
+    }
+}
 
 
 // Claims the next work item for the block (thread 0: first + t stride for
@@ -321,17 +356,28 @@ __device__ inline void dep_item(const DiscArgs &a, SegSmem<RCH> &sm, int r0, int
                                 float *plane) {
     const Ext e = sm.h.ext;
     seg_build<BT, RCH>(a, sm, r0, n, POLY);
-    seg_walk<RCH, kDepLanes>(
-        sm, n,
-        [&](const SRun &r, int j, bool second) {
+    if constexpr (kDepSectors) {
+        seg_walk_sectors<RCH>(sm, n, [&](const SRun &r, int j, bool in0, bool in1) {
             const float jf = (float)j;
-            const float2 w = seg_weight2<POLY>(e, r, make_float2(jf, jf + (float)kDepLanes));
+            const float2 w = seg_weight2<POLY>(e, r, make_float2(jf, jf + 8.0f));
             const float2 p = fma2(w, f2(F), mul2(w, f2(Flo)));   // w (F + Flo), rounded once
             float *const m = plane + (r.pix0 + j);
-            red_add_f32(m, p.x);
-            if (second) red_add_f32(m + kDepLanes, p.y);
-        },
-        []() {});
+            if (in0) red_add_f32(m, p.x);
+            if (in1) red_add_f32(m + 8, p.y);
+        });
+    } else {
+        seg_walk<RCH, kDepLanes>(
+            sm, n,
+            [&](const SRun &r, int j, bool second) {
+                const float jf = (float)j;
+                const float2 w = seg_weight2<POLY>(e, r, make_float2(jf, jf + (float)kDepLanes));
+                const float2 p = fma2(w, f2(F), mul2(w, f2(Flo)));   // w (F + Flo), rounded once
+                float *const m = plane + (r.pix0 + j);
+                red_add_f32(m, p.x);
+                if (second) red_add_f32(m + kDepLanes, p.y);
+            },
+            []() {});
+    }
     __syncthreads();
 }
 
