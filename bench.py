@@ -473,11 +473,53 @@ def run_gb300(args, ws, rank, local):
     if not args.no_extras and rank == 0:
         del dparts, dmap
         torch.cuda.empty_cache()
+        line["small_map"] = bench_small(dev, args)
         line["batched"] = bench_batched(dev)
         line["adjoint"] = bench_adjoint(dev)
         line["large_map"] = bench_large(dev)
     if rank == 0:
         print(json.dumps(line), flush=True)
+
+
+def bench_small(dev, args):
+    """The plain method's own configuration: 1,048,576 NFW particles at Nside
+    512, rendered whole by both GPU forms (CUDA events after a warm-up: one
+    plain render, the median of three compensated ones; inputs resident),
+    each against the FP64 oracle on a sample, and the oracle (the restated
+    reference CPU path) timed on the host cores."""
+    import torch
+    import annmap
+    from annmap import synth
+    P, nside = synth.workload("nfw1m_ns512")
+    n, npix = len(P), 12 * nside * nside
+    r = annmap.Renderer(dev.index or 0)
+    r.set_params(annmap.Parameters.for_synthetic(P, nside))
+    dparts = {k: torch.from_numpy(v).to(dev) for k, v in P.as_dict().items()}
+    out = torch.empty(npix, dtype=torch.float64, device=dev)
+    res = {"workload": "nfw1m_ns512", "particles": n, "nside": nside}
+    for name, prec, reps in (("plain_f64", annmap.PLAIN_F64, 1), ("comp_f32", annmap.COMP_F32, 3)):
+        r.render(dparts, nside, prec, out=out)   # warm-up
+        ms = []
+        for _ in range(reps):
+            r.render(dparts, nside, prec, out=out)
+            torch.cuda.synchronize()
+            ms.append(r.stats()["kernel_ms"])
+        t = statistics.median(ms)
+        st = r.stats()
+        res[name] = {"ms": t, "particles_per_s": n / (t / 1e3), "deposits": st["deposits"],
+                     "deposits_per_s": st["deposits"] / (t / 1e3)}
+    cpu, csub, omap, otot = cpu_oracle_run(P, nside, min(10.0, args.cpu_seconds))
+    res["cpu_baseline"] = {"value": cpu["value"], "unit": UNIT, "cores": cpu["cores"], "kind": "port",
+                           "deposits_per_s": cpu["deposits_per_s"],
+                           "sample": f"{cpu['particles']} particles, {cpu['seconds']:.1f} s"}
+    dom = 4 * math.pi / npix
+    for name, prec in (("plain_f64", annmap.PLAIN_F64), ("comp_f32", annmap.COMP_F32)):
+        g = r.render(csub.as_dict(), nside, prec)
+        med, mx = rel_err(g, omap)
+        res[name]["px_err_vs_oracle"] = {"particles": cpu["particles"], "median": med, "max": mx,
+                                         "total_flux_rel": abs(g.sum() * dom - otot) / otot}
+    r.close()
+    return res
 
 
 def bench_batched(dev):

@@ -345,12 +345,24 @@ __global__ void __launch_bounds__(kWPBA * 32) k_adjc_warp(adj::AdjArgs a) {
 // The headers of every disc in the queue, one thread per particle (the
 // FP64 set-up at full warp width instead of on one lane of a waiting block).
 __global__ void __launch_bounds__(256) k_comp_hdr(DiscArgs a) {
+    // each warp builds its 32 consecutive headers in shared memory and
+    // stores them as one contiguous run of 16-byte words (a thread's own
+    // 160-byte store would leave partial sectors for the L2 to merge)
+    constexpr int kW16 = sizeof(CompHdr) / 16;
+    static_assert(sizeof(CompHdr) % 16 == 0, "headers are stored in 16-byte words");
+    __shared__ __align__(16) CompHdr stage[8][32];
     const long long ndisc = a.ctr[C_ADD_DISC];
     const long long stride = (long long)gridDim.x * blockDim.x;
-    for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < ndisc; q += stride) {
-        CompHdr h;
-        setup_hdr(a, a.queue[q], h);
-        a.chdr[q] = h;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (long long q0 = (long long)blockIdx.x * blockDim.x + (threadIdx.x & ~31); q0 < ndisc; q0 += stride) {
+        const long long q = q0 + lane;
+        if (q < ndisc) setup_hdr(a, a.queue[q], stage[w][lane]);
+        __syncwarp();
+        const int nh = (int)min(32LL, ndisc - q0);
+        const float4 *src = reinterpret_cast<const float4 *>(&stage[w][0]);
+        float4 *dst = reinterpret_cast<float4 *>(a.chdr + q0);
+        for (int k = lane; k < nh * kW16; k += 32) dst[k] = src[k];
+        __syncwarp();
     }
 }
 

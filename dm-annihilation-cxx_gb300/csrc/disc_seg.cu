@@ -213,45 +213,14 @@ __device__ inline void seg_walk(SegSmem<RCH> &sm, int n, Body body, Done ring_do
     }
 }
 
-constexpr int kNormLanes = 8;    // lanes per ring in pass 1 (weights only)
-constexpr int kDepLanes = 32;    // lanes per ring in pass 2's run walk
+// Lanes per ring.  Pass 1 (weights only) walks eight rings per warp: measured
+// on the 16M workload at Nside 2048, 4 / 8 / 16 / 32 lanes per ring took
+// 435 / 460 / 519 / 627 ms.  Pass 2 keeps whole warps on a ring, so a warp's
+// reduction covers 32 consecutive floats: 16 lanes per ring, or eight lanes
+// on aligned 32-byte sectors, measured slower (760 and 826 ms against 753).
+constexpr int kNormLanes = 4;
+constexpr int kDepLanes = 32;
 constexpr int kFoldPairs = 8;    // pass 1, large discs: pixel pairs per plain FP32 partial
-constexpr bool kDepSectors = true;   // pass 2 walks 32-byte sectors (seg_walk_sectors)
-
-// Pass 2's sector walk: warps claim four rings at a time, eight lanes per
-// ring, and lane l of a group takes map pixel 8 m + l of every 32-byte
-// sector m the run touches (two sectors per step: pixels j and j + 8), so
-// each group's reduction instruction covers exactly one aligned sector --
-// the fewest L2 sectors per deposit a scalar FP32 reduction can reach --
-// while the per-ring work is shared by four rings as in pass 1.
-// body(run, j, in0, in1) gets the run-local index j of the lane's first
-// pixel (negative before the run) and whether j and j + 8 are in the run.
-template <int RCH, class Body>
-__device__ inline void seg_walk_sectors(SegSmem<RCH> &sm, int n, Body body) {
-    const int lane = threadIdx.x & 31, sl = lane & 7;
-    int q0 = 0;
-    if (lane == 0) q0 = atomicAdd(&sm.next_run, 4);
-    q0 = __shfl_sync(0xffffffffu, q0, 0);
-    while (q0 < n) {
-        int qn = 0;
-        if (lane == 0) qn = atomicAdd(&sm.next_run, 4);
-        const int q = q0 + (lane >> 3);
-        if (q < n) {
-#pragma unroll 1
-            for (int k = 0; k < 2; k++) {
-                if (k == 1 && !sm.run[2 * q].more) break;
-                const SRun r = sm.run[2 * q + k];
-                const int a0 = r.pix0 >> 3, ns = ((r.pix0 + r.cnt + 7) >> 3) - a0;
-                for (int t = 0; t < ns; t += 2) {
-                    const int j = ((a0 + t) << 3) + sl - r.pix0;
-                    body(r, j, (unsigned)j < (unsigned)r.cnt, (unsigned)(j + 8) < (unsigned)r.cnt);
-                }
-            }
-        }
-        q0 = __shfl_sync(0xffffffffu, qn, 0);
-    }
-}
-
 
 // Claims the next work item for the block (thread 0: first + t stride for
 // the t-th claim, below end) and stages its disc's header; false when the
@@ -356,28 +325,17 @@ __device__ inline void dep_item(const DiscArgs &a, SegSmem<RCH> &sm, int r0, int
                                 float *plane) {
     const Ext e = sm.h.ext;
     seg_build<BT, RCH>(a, sm, r0, n, POLY);
-    if constexpr (kDepSectors) {
-        seg_walk_sectors<RCH>(sm, n, [&](const SRun &r, int j, bool in0, bool in1) {
+    seg_walk<RCH, kDepLanes>(
+        sm, n,
+        [&](const SRun &r, int j, bool second) {
             const float jf = (float)j;
-            const float2 w = seg_weight2<POLY>(e, r, make_float2(jf, jf + 8.0f));
+            const float2 w = seg_weight2<POLY>(e, r, make_float2(jf, jf + (float)kDepLanes));
             const float2 p = fma2(w, f2(F), mul2(w, f2(Flo)));   // w (F + Flo), rounded once
             float *const m = plane + (r.pix0 + j);
-            if (in0) red_add_f32(m, p.x);
-            if (in1) red_add_f32(m + 8, p.y);
-        });
-    } else {
-        seg_walk<RCH, kDepLanes>(
-            sm, n,
-            [&](const SRun &r, int j, bool second) {
-                const float jf = (float)j;
-                const float2 w = seg_weight2<POLY>(e, r, make_float2(jf, jf + (float)kDepLanes));
-                const float2 p = fma2(w, f2(F), mul2(w, f2(Flo)));   // w (F + Flo), rounded once
-                float *const m = plane + (r.pix0 + j);
-                red_add_f32(m, p.x);
-                if (second) red_add_f32(m + kDepLanes, p.y);
-            },
-            []() {});
-    }
+            red_add_f32(m, p.x);
+            if (second) red_add_f32(m + kDepLanes, p.y);
+        },
+        []() {});
     __syncthreads();
 }
 
@@ -423,25 +381,38 @@ template <int RCH>
 __global__ void __launch_bounds__(256) k_seg_count(DiscArgs a, SegArgs sg) {
     const long long nblk = a.ctr[C_ADD_BLOCK];
     const long long stride = (long long)gridDim.x * blockDim.x;
+    const int lane = threadIdx.x & 31;
     long long est_sum = 0;
-    for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < nblk; q += stride) {
-        CompHdr &h = a.chdr[q];
-        const int nring = max(1, h.hdr.r_last - h.hdr.r_first + 1);
-        const double est = disc_npix_estimate(a.g, h.hdr.ar);
-        const double per_ring = est / nring;
-        int rpi = per_ring > 0.0 ? (int)min((double)RCH, (double)kItemPx / per_ring) : RCH;
-        rpi = max(1, min(RCH, rpi));
-        const int nit = (nring + rpi - 1) / rpi;
-        h.ext.rpi = rpi;
-        sg.disc_first[q] = (long long)atomicAdd((unsigned long long *)(a.ctr + C_SEG_ITEMS),
-                                                (unsigned long long)nit);
-        sg.disc_nitems[q] = nit;
-        sg.disc_S[q] = 0.0;
-        sg.disc_px[q] = 0;
-        est_sum += (long long)est;
+    // warp-uniform trips: the warp claims its 32 discs' items with one atomic
+    for (long long q0 = (long long)blockIdx.x * blockDim.x + (threadIdx.x & ~31); q0 < nblk; q0 += stride) {
+        const long long q = q0 + lane;
+        int nit = 0;
+        if (q < nblk) {
+            CompHdr &h = a.chdr[q];
+            const int nring = max(1, h.hdr.r_last - h.hdr.r_first + 1);
+            const double est = disc_npix_estimate(a.g, h.hdr.ar);
+            const double per_ring = est / nring;
+            int rpi = per_ring > 0.0 ? (int)min((double)RCH, (double)kItemPx / per_ring) : RCH;
+            rpi = max(1, min(RCH, rpi));
+            nit = (nring + rpi - 1) / rpi;
+            h.ext.rpi = rpi;
+            sg.disc_S[q] = 0.0;
+            sg.disc_px[q] = 0;
+            est_sum += (long long)est;
+        }
+        int tot;
+        const int ex = warp_excl_scan(nit, tot);
+        unsigned long long base = 0;
+        if (lane == 0 && tot > 0)
+            base = atomicAdd((unsigned long long *)(a.ctr + C_SEG_ITEMS), (unsigned long long)tot);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (q < nblk) {
+            sg.disc_first[q] = (long long)base + ex;
+            sg.disc_nitems[q] = nit;
+        }
     }
     est_sum = warp_sum_ll(est_sum);
-    if ((threadIdx.x & 31) == 0 && est_sum)
+    if (lane == 0 && est_sum)
         atomicAdd((unsigned long long *)(a.ctr + C_SEG_EST), (unsigned long long)est_sum);
 }
 
