@@ -181,8 +181,8 @@ __device__ __forceinline__ float2 seg_weight2(const Ext &e, const SRun &r, float
 
 // Warps claim 32 / S consecutive rings (both slots of each) of the staged
 // item at a time, one ring per group of S lanes, and call
-// body(run, j, second) for pixels j and j + S of the ring (second: j + S is
-// inside), so the per-ring work of the walk (the claim, the run's loads,
+// body(run, j, S, second) for pixels j and j + S of the ring (second: j + S
+// is inside), so the per-ring work of the walk (the claim, the run's loads,
 // the loop set-up, ring_done) is shared by the rings a warp walks together;
 // neighbouring rings of a disc have similar lengths, so the groups finish
 // together.  The S lanes of a group touch S consecutive pixels (S floats of
@@ -202,15 +202,43 @@ __device__ inline void seg_walk(SegSmem<RCH> &sm, int n, Body body, Done ring_do
         const int q = q0 + lane / S;
         if (q < n) {
             const SRun r = sm.run[2 * q];
-            for (int j = sl; j < r.cnt; j += 2 * S) body(r, j, j + S < r.cnt);
+            for (int j = sl; j < r.cnt; j += 2 * S) body(r, j, S, j + S < r.cnt);
             if (r.more) {
                 const SRun r2 = sm.run[2 * q + 1];
-                for (int j = sl; j < r2.cnt; j += 2 * S) body(r2, j, j + S < r2.cnt);
+                for (int j = sl; j < r2.cnt; j += 2 * S) body(r2, j, S, j + S < r2.cnt);
             }
         }
         ring_done();
         q0 = __shfl_sync(0xffffffffu, qn, 0);
     }
+}
+
+// The whole block on one ring at a time (items of a few long rings: the
+// discs of hundreds of degrees): thread t takes pixels t, t + BT of every
+// 2 BT; body(run, j, BT, second) as in seg_walk, ring_done() after each ring.
+template <int BT, int RCH, class Body, class Done>
+__device__ inline void seg_walk_block(SegSmem<RCH> &sm, int n, Body body, Done ring_done) {
+    for (int q = 0; q < n; q++) {
+        const SRun r = sm.run[2 * q];
+        for (int j = threadIdx.x; j < r.cnt; j += 2 * BT) body(r, j, BT, j + BT < r.cnt);
+        if (r.more) {
+            const SRun r2 = sm.run[2 * q + 1];
+            for (int j = threadIdx.x; j < r2.cnt; j += 2 * BT) body(r2, j, BT, j + BT < r2.cnt);
+        }
+        ring_done();
+    }
+}
+
+// The walk for an item of n rings: S lanes per ring, the smallest of
+// S0 .. 32 that keeps every lane group of the block on a ring (n >= BT / S),
+// else the whole block on each ring in turn.
+template <int BT, int RCH, int S0, class Body, class Done>
+__device__ inline void seg_walk_any(SegSmem<RCH> &sm, int n, Body body, Done ring_done) {
+    if (S0 <= 4 && n >= BT / 4) seg_walk<RCH, 4>(sm, n, body, ring_done);
+    else if (S0 <= 8 && n >= BT / 8) seg_walk<RCH, 8>(sm, n, body, ring_done);
+    else if (S0 <= 16 && n >= BT / 16) seg_walk<RCH, 16>(sm, n, body, ring_done);
+    else if (n >= BT / 32) seg_walk<RCH, 32>(sm, n, body, ring_done);
+    else seg_walk_block<BT, RCH>(sm, n, body, ring_done);
 }
 
 // Lanes per ring.  Pass 1 (weights only) walks eight rings per warp: measured
@@ -271,11 +299,11 @@ __device__ inline void norm_item(const DiscArgs &a, SegSmem<RCH> &sm, int r0, in
         part = f2(0.0f);
         np = 0;
     };
-    seg_walk<RCH, kNormLanes>(
+    seg_walk_any<BT, RCH, kNormLanes>(
         sm, n,
-        [&](const SRun &r, int j, bool second) {
+        [&](const SRun &r, int j, int off, bool second) {
             const float jf = (float)j;
-            float2 w = seg_weight2<POLY>(e, r, make_float2(jf, jf + (float)kNormLanes));
+            float2 w = seg_weight2<POLY>(e, r, make_float2(jf, jf + (float)off));
             if (!second) w.y = 0.0f;
             part = add2(part, w);
             // the large discs' rings are long (up to the whole ring): keep the
@@ -325,15 +353,15 @@ __device__ inline void dep_item(const DiscArgs &a, SegSmem<RCH> &sm, int r0, int
                                 float *plane) {
     const Ext e = sm.h.ext;
     seg_build<BT, RCH>(a, sm, r0, n, POLY);
-    seg_walk<RCH, kDepLanes>(
+    seg_walk_any<BT, RCH, kDepLanes>(
         sm, n,
-        [&](const SRun &r, int j, bool second) {
+        [&](const SRun &r, int j, int off, bool second) {
             const float jf = (float)j;
-            const float2 w = seg_weight2<POLY>(e, r, make_float2(jf, jf + (float)kDepLanes));
+            const float2 w = seg_weight2<POLY>(e, r, make_float2(jf, jf + (float)off));
             const float2 p = fma2(w, f2(F), mul2(w, f2(Flo)));   // w (F + Flo), rounded once
             float *const m = plane + (r.pix0 + j);
             red_add_f32(m, p.x);
-            if (second) red_add_f32(m + kDepLanes, p.y);
+            if (second) red_add_f32(m + off, p.y);
         },
         []() {});
     __syncthreads();
