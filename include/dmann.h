@@ -239,8 +239,13 @@ dmann_status dmann_map_add_v(dmann_ctx *ctx, const float *x, const float *y,
  * the frame rot[9k..9k+8] / opos[3k..3k+2] (as dmann_set_frame) and its own
  * nside[k]; its map goes to maps[k] (12*nside[k]^2 doubles, host or device).
  * The particles are uploaded once; when every map is a device pointer the
- * whole batch is captured into one CUDA graph and launched once.  Returns when
- * all maps are complete.  The context's own frame is left unchanged. */
+ * whole batch is captured into one CUDA graph and launched once.  The context
+ * keeps that graph: a later batch with the same inputs, maps, frames, Nside
+ * values, units and tuning (and no context buffer reallocated since) launches
+ * it again without capturing; one with other frames or maps updates it in
+ * place where the graph's shape allows.  Returns when all maps are complete;
+ * dmann_get_stats then reports the counters summed over the observers and
+ * the graph's device time.  The context's own frame is left unchanged. */
 dmann_status dmann_render_batch(dmann_ctx *ctx, const float *x, const float *y,
                                 const float *z, const float *m, const float *rho,
                                 const float *h, int64_t n, int n_obs,
