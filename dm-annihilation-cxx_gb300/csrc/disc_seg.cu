@@ -190,7 +190,7 @@ __device__ __forceinline__ float2 seg_weight2(const Ext &e, const SRun &r, float
 // each claim.
 template <int RCH, int S, class Body, class Done>
 __device__ inline void seg_walk(SegSmem<RCH> &sm, int n, Body body, Done ring_done) {
-    static_assert(S == 4 || S == 8 || S == 16 || S == 32, "lanes per ring");
+    static_assert(S == 2 || S == 4 || S == 8 || S == 16 || S == 32, "lanes per ring");
     constexpr int G = 32 / S;
     const int lane = threadIdx.x & 31, sl = lane % S;
     int q0 = 0;
@@ -234,7 +234,8 @@ __device__ inline void seg_walk_block(SegSmem<RCH> &sm, int n, Body body, Done r
 // else the whole block on each ring in turn.
 template <int BT, int RCH, int S0, class Body, class Done>
 __device__ inline void seg_walk_any(SegSmem<RCH> &sm, int n, Body body, Done ring_done) {
-    if (S0 <= 4 && n >= BT / 4) seg_walk<RCH, 4>(sm, n, body, ring_done);
+    if (S0 <= 2 && n >= BT / 2) seg_walk<RCH, 2>(sm, n, body, ring_done);
+    else if (S0 <= 4 && n >= BT / 4) seg_walk<RCH, 4>(sm, n, body, ring_done);
     else if (S0 <= 8 && n >= BT / 8) seg_walk<RCH, 8>(sm, n, body, ring_done);
     else if (S0 <= 16 && n >= BT / 16) seg_walk<RCH, 16>(sm, n, body, ring_done);
     else if (n >= BT / 32) seg_walk<RCH, 32>(sm, n, body, ring_done);
