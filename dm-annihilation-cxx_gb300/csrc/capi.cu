@@ -34,6 +34,19 @@ struct RingTables {
 
 }  // namespace
 
+// One map's device work: the prep outputs, the queue, the counters and
+// accumulation planes, the disc headers and the segmented render's buffers.
+// A context renders with work[0]; a batch of device maps uses both, one
+// observer on each at a time.
+struct Work {
+    DevBuf theta, phi, ar, flux, cpix, key, queue, hist, ctr, fsum, acc;
+    DevBuf chdr;              // the compensated form's disc headers, one per queue slot
+    // segmented render (disc_seg.cu): work items, per-disc item ranges,
+    // weight sums and pixel counts, and the FP32 deposit plane
+    DevBuf seg_items, seg_sorted, seg_cls, seg_first, seg_nit, seg_S, seg_px, plane32;
+    bool seg_plane = false;   // plane32 holds a zeroed plane for the open map
+};
+
 struct dmann_ctx {
     int device = 0;
     int num_sms = 0;
@@ -55,15 +68,15 @@ struct dmann_ctx {
     dmann_tuning tune{};
     std::map<int, dmann_tuning> tune_ns;   // per-Nside overrides (the autotuner's table)
     std::map<int, RingTables> rings;
-    // workspace
-    DevBuf in[7], theta, phi, ar, flux, cpix, key, queue, hist, ctr, fsum, acc, map;
+    // workspace: the staged inputs and map, the adjoint's buffers, and the
+    // per-map work (w: work[0], or a batch lane's)
+    DevBuf in[7], map;
     DevBuf cls, oacc, grad;   // the adjoint's class array, observer sums, staged gradient
     DevBuf core_gln;          // the adjoint's d ln(halo-core factor) / d pos, [3][n]
-    DevBuf chdr;              // the compensated form's disc headers, one per queue slot
-    // segmented render (disc_seg.cu): work items, per-disc item ranges,
-    // weight sums and pixel counts, and the FP32 deposit plane
-    DevBuf seg_items, seg_sorted, seg_cls, seg_first, seg_nit, seg_S, seg_px, plane32;
-    bool seg_plane = false;       // plane32 holds a zeroed plane for the open map
+    Work work[2];
+    Work *w = &work[0];
+    cudaStream_t lane_stream = nullptr;   // the batch's second lane
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     // dmann_render_batch: the instantiated graph of the last batch of device
     // maps and the parameters it was captured with (relaunched when a batch
     // repeats them), and the batch's counters summed over its observers
@@ -127,18 +140,18 @@ std::atomic<unsigned long long> g_alloc_gen{0};
 
 void reserve_headers(dmann_ctx *ctx, size_t n) {
     const size_t bytes = comp_hdr_bytes() * (n > 0 ? n : 1);
-    if (ctx->chdr.bytes >= bytes) return;
-    if (ctx->chdr.p) cudaFree(ctx->chdr.p);
-    ctx->chdr.p = nullptr;
-    ctx->chdr.bytes = 0;
+    if (ctx->w->chdr.bytes >= bytes) return;
+    if (ctx->w->chdr.p) cudaFree(ctx->w->chdr.p);
+    ctx->w->chdr.p = nullptr;
+    ctx->w->chdr.bytes = 0;
     ++g_alloc_gen;
     for (size_t want : {bytes + bytes / 8, bytes}) {
-        if (cudaMalloc(&ctx->chdr.p, want) == cudaSuccess) {
-            ctx->chdr.bytes = want;
+        if (cudaMalloc(&ctx->w->chdr.p, want) == cudaSuccess) {
+            ctx->w->chdr.bytes = want;
             return;
         }
         cudaGetLastError();
-        ctx->chdr.p = nullptr;
+        ctx->w->chdr.p = nullptr;
     }
 }
 
@@ -162,8 +175,8 @@ bool ensure_opt(DevBuf &b, size_t bytes) {
 }
 
 CompHdr *headers_for(const dmann_ctx *ctx, size_t n) {
-    const bool fits = ctx->chdr.p && ctx->chdr.bytes >= comp_hdr_bytes() * (n > 0 ? n : 1);
-    return fits ? (CompHdr *)ctx->chdr.p : nullptr;
+    const bool fits = ctx->w->chdr.p && ctx->w->chdr.bytes >= comp_hdr_bytes() * (n > 0 ? n : 1);
+    return fits ? (CompHdr *)ctx->w->chdr.p : nullptr;
 }
 
 dmann_status ensure(dmann_ctx *ctx, DevBuf &b, size_t bytes) {
@@ -348,13 +361,18 @@ void dmann_destroy(dmann_ctx *ctx) {
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
     DevBuf *bufs[] = {&ctx->in[0], &ctx->in[1], &ctx->in[2], &ctx->in[3], &ctx->in[4], &ctx->in[5],
-                      &ctx->in[6],
-                      &ctx->theta, &ctx->phi, &ctx->ar, &ctx->flux, &ctx->cpix, &ctx->key,
-                      &ctx->queue, &ctx->hist, &ctx->ctr, &ctx->fsum, &ctx->acc, &ctx->map,
-                      &ctx->cls, &ctx->oacc, &ctx->grad, &ctx->halo_f, &ctx->halo_cells,
-                      &ctx->corr, &ctx->chdr, &ctx->core_gln, &ctx->seg_items, &ctx->seg_sorted,
-                      &ctx->seg_cls, &ctx->seg_first,
-                      &ctx->seg_nit, &ctx->seg_S, &ctx->seg_px, &ctx->plane32, &ctx->bstats};
+                      &ctx->in[6], &ctx->map, &ctx->cls, &ctx->oacc, &ctx->grad, &ctx->halo_f,
+                      &ctx->halo_cells, &ctx->corr, &ctx->core_gln, &ctx->bstats};
+    for (Work &wk : ctx->work) {
+        DevBuf *wb[] = {&wk.theta, &wk.phi, &wk.ar, &wk.flux, &wk.cpix, &wk.key, &wk.queue, &wk.hist,
+                        &wk.ctr, &wk.fsum, &wk.acc, &wk.chdr, &wk.seg_items, &wk.seg_sorted,
+                        &wk.seg_cls, &wk.seg_first, &wk.seg_nit, &wk.seg_S, &wk.seg_px, &wk.plane32};
+        for (DevBuf *b : wb)
+            if (b->p) cudaFree(b->p);
+    }
+    if (ctx->lane_stream) cudaStreamDestroy(ctx->lane_stream);
+    if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
+    if (ctx->ev_join) cudaEventDestroy(ctx->ev_join);
     if (ctx->batch_exec) cudaGraphExecDestroy(ctx->batch_exec);
     for (DevBuf *b : bufs)
         if (b->p) cudaFree(b->p);
@@ -632,7 +650,7 @@ bool law_needs_sigmav(int model) {
 
 Accum make_accum(dmann_ctx *ctx) {
     Accum acc;
-    acc.acc64 = (double *)ctx->acc.p;
+    acc.acc64 = (double *)ctx->w->acc.p;
     return acc;
 }
 
@@ -651,24 +669,24 @@ size_t seg_capacity(size_t n) { return 4 * (n > 0 ? n : 1) + ((size_t)1 << 20); 
 // when an allocation fails; nothing is allocated when they are big enough).
 bool reserve_seg(dmann_ctx *ctx, size_t n) {
     const size_t n1 = n > 0 ? n : 1, cap = seg_capacity(n);
-    return ensure_opt(ctx->seg_first, 8 * n1) && ensure_opt(ctx->seg_nit, 4 * n1) &&
-           ensure_opt(ctx->seg_S, 8 * n1) && ensure_opt(ctx->seg_px, 8 * n1) &&
-           ensure_opt(ctx->seg_cls, kSegBufBytes) && ensure_opt(ctx->seg_items, 8 * cap) &&
-           ensure_opt(ctx->seg_sorted, 8 * cap);
+    return ensure_opt(ctx->w->seg_first, 8 * n1) && ensure_opt(ctx->w->seg_nit, 4 * n1) &&
+           ensure_opt(ctx->w->seg_S, 8 * n1) && ensure_opt(ctx->w->seg_px, 8 * n1) &&
+           ensure_opt(ctx->w->seg_cls, kSegBufBytes) && ensure_opt(ctx->w->seg_items, 8 * cap) &&
+           ensure_opt(ctx->w->seg_sorted, 8 * cap);
 }
 
 dmann_status render_segmented(dmann_ctx *ctx, const DiscArgs &da, const dmann_tuning &tu, size_t N,
                               bool &used, bool timed = true) {
     used = false;
-    if (!da.chdr || !ctx->seg_plane || !reserve_seg(ctx, N)) return DMANN_OK;
+    if (!da.chdr || !ctx->w->seg_plane || !reserve_seg(ctx, N)) return DMANN_OK;
     const size_t cap = seg_capacity(N);
     cudaStream_t s = ctx->stream;
     const int bt = tu.block_threads == 128 ? 128 : 256;
     const int lg = tu.seg_min_deposits_log2 > 0 ? tu.seg_min_deposits_log2 : 28;
-    char *buf = (char *)ctx->seg_cls.p;
+    char *buf = (char *)ctx->w->seg_cls.p;
     SegArgs sg{};
-    sg.items = (int2 *)ctx->seg_items.p;
-    sg.sorted = (int2 *)ctx->seg_sorted.p;
+    sg.items = (int2 *)ctx->w->seg_items.p;
+    sg.sorted = (int2 *)ctx->w->seg_sorted.p;
     sg.cap = (long long)cap;
     sg.cls = (int *)buf;
     sg.cls_px = (long long *)(buf + kSegClsBytes);
@@ -677,11 +695,11 @@ dmann_status render_segmented(dmann_ctx *ctx, const DiscArgs &da, const dmann_tu
     sg.ctl = (int *)(buf + kSegClsBytes + kSegClsPxBytes + kSegNextBytes + kSegSpanBytes);
     sg.min_est = 1LL << lg;
     sg.budget = (long long)ctx->g.npix * kDepPerPix;
-    sg.disc_first = (long long *)ctx->seg_first.p;
-    sg.disc_nitems = (int *)ctx->seg_nit.p;
-    sg.disc_S = (double *)ctx->seg_S.p;
-    sg.disc_px = (long long *)ctx->seg_px.p;
-    sg.plane = (float *)ctx->plane32.p;
+    sg.disc_first = (long long *)ctx->w->seg_first.p;
+    sg.disc_nitems = (int *)ctx->w->seg_nit.p;
+    sg.disc_S = (double *)ctx->w->seg_S.p;
+    sg.disc_px = (long long *)ctx->w->seg_px.p;
+    sg.plane = (float *)ctx->w->plane32.p;
     CK(cudaMemsetAsync(buf, 0, kSegBufBytes, s));
     CK(launch_hdr(da, ctx->num_sms, s));
     CK(launch_seg_count(da, sg, bt, ctx->num_sms, s));
@@ -726,18 +744,18 @@ dmann_status dmann_map_begin(dmann_ctx *ctx, int nside, int precision) {
     ctx->precision = precision;
     if ((st = ring_tables(ctx, nside, ctx->rt)) != DMANN_OK) return st;
     const size_t P = (size_t)ctx->g.npix;
-    if ((st = ensure(ctx, ctx->acc, 8 * P)) || (st = ensure(ctx, ctx->hist, 4 * (size_t)kKeys)) ||
-        (st = ensure(ctx, ctx->ctr, 8 * C_COUNT)) || (st = ensure(ctx, ctx->fsum, 8)))
+    if ((st = ensure(ctx, ctx->w->acc, 8 * P)) || (st = ensure(ctx, ctx->w->hist, 4 * (size_t)kKeys)) ||
+        (st = ensure(ctx, ctx->w->ctr, 8 * C_COUNT)) || (st = ensure(ctx, ctx->w->fsum, 8)))
         return st;
     cudaStream_t s = ctx->stream;
     CK(cudaEventRecord(ctx->ev0, s));
-    CK(cudaMemsetAsync(ctx->acc.p, 0, 8 * P, s));
-    CK(cudaMemsetAsync(ctx->ctr.p, 0, 8 * C_COUNT, s));
-    CK(cudaMemsetAsync(ctx->fsum.p, 0, 8, s));
+    CK(cudaMemsetAsync(ctx->w->acc.p, 0, 8 * P, s));
+    CK(cudaMemsetAsync(ctx->w->ctr.p, 0, 8 * C_COUNT, s));
+    CK(cudaMemsetAsync(ctx->w->fsum.p, 0, 8, s));
     // the segmented render's FP32 plane: zero at the start of a map, and
     // every segment's flush leaves it zero
-    ctx->seg_plane = precision == DMANN_COMP_F32 && ensure_opt(ctx->plane32, 4 * P);
-    if (ctx->seg_plane) CK(cudaMemsetAsync(ctx->plane32.p, 0, 4 * P, s));
+    ctx->w->seg_plane = precision == DMANN_COMP_F32 && ensure_opt(ctx->w->plane32, 4 * P);
+    if (ctx->w->seg_plane) CK(cudaMemsetAsync(ctx->w->plane32.p, 0, 4 * P, s));
     ctx->stats = dmann_stats{};
     ctx->launches = 0;
     ctx->disc_timed = false;
@@ -765,10 +783,10 @@ dmann_status dmann_map_add_v(dmann_ctx *ctx, const float *x, const float *y, con
     CK(cudaSetDevice(ctx->device));
     cudaStream_t s = ctx->stream;
     const size_t N = (size_t)n;
-    if ((st = ensure(ctx, ctx->theta, 8 * N)) || (st = ensure(ctx, ctx->phi, 8 * N)) ||
-        (st = ensure(ctx, ctx->ar, 8 * N)) || (st = ensure(ctx, ctx->flux, 8 * N)) ||
-        (st = ensure(ctx, ctx->cpix, 4 * N)) || (st = ensure(ctx, ctx->key, 4 * N)) ||
-        (st = ensure(ctx, ctx->queue, 4 * N)))
+    if ((st = ensure(ctx, ctx->w->theta, 8 * N)) || (st = ensure(ctx, ctx->w->phi, 8 * N)) ||
+        (st = ensure(ctx, ctx->w->ar, 8 * N)) || (st = ensure(ctx, ctx->w->flux, 8 * N)) ||
+        (st = ensure(ctx, ctx->w->cpix, 4 * N)) || (st = ensure(ctx, ctx->w->key, 4 * N)) ||
+        (st = ensure(ctx, ctx->w->queue, 4 * N)))
         return st;
     if (ctx->precision == DMANN_COMP_F32) reserve_headers(ctx, N);
     // inputs: device pointers are used in place, host arrays are copied
@@ -790,8 +808,8 @@ dmann_status dmann_map_add_v(dmann_ctx *ctx, const float *x, const float *y, con
     const dmann_tuning &tu = tuning_for(ctx, ctx->g.nside);
     const int bmin = block_bucket_min(tu);
 
-    CK(cudaMemsetAsync(ctx->hist.p, 0, 4 * (size_t)kKeys, s));
-    CK(cudaMemsetAsync((long long *)ctx->ctr.p + kCtrChunkFirst, 0, 8 * (C_COUNT - kCtrChunkFirst), s));
+    CK(cudaMemsetAsync(ctx->w->hist.p, 0, 4 * (size_t)kKeys, s));
+    CK(cudaMemsetAsync((long long *)ctx->w->ctr.p + kCtrChunkFirst, 0, 8 * (C_COUNT - kCtrChunkFirst), s));
     PrepArgs pa;
     pa.p = {dev[0], dev[1], dev[2], dev[3], dev[4], dev[5], (int)N, dev[6]};
     pa.core_corr = nullptr;
@@ -804,18 +822,18 @@ dmann_status dmann_map_add_v(dmann_ctx *ctx, const float *x, const float *y, con
     }
     pa.f = f;
     pa.g = ctx->g;
-    pa.out = {(double *)ctx->theta.p, (double *)ctx->phi.p, (double *)ctx->ar.p,
-              (double *)ctx->flux.p, (int *)ctx->cpix.p, (int *)ctx->key.p};
-    pa.hist = (int *)ctx->hist.p;
-    pa.ctr = (long long *)ctx->ctr.p;
-    pa.flux_sum = (double *)ctx->fsum.p;
+    pa.out = {(double *)ctx->w->theta.p, (double *)ctx->w->phi.p, (double *)ctx->w->ar.p,
+              (double *)ctx->w->flux.p, (int *)ctx->w->cpix.p, (int *)ctx->w->key.p};
+    pa.hist = (int *)ctx->w->hist.p;
+    pa.ctr = (long long *)ctx->w->ctr.p;
+    pa.flux_sum = (double *)ctx->w->fsum.p;
     pa.acc = acc;
     pa.precision = ctx->precision;
     pa.block_bucket_min = bmin;
     pa.deposit_singles = 1;
     CK(launch_prep(pa, s));
     CK(launch_scan(pa.hist, pa.ctr, bmin, s));
-    CK(launch_scatter(pa, (int *)ctx->queue.p, s));
+    CK(launch_scatter(pa, (int *)ctx->w->queue.p, s));
 
     DiscArgs da;
     da.g = ctx->g;
@@ -826,7 +844,7 @@ dmann_status dmann_map_add_v(dmann_ctx *ctx, const float *x, const float *y, con
     da.ar = pa.out.ar;
     da.flux = pa.out.flux;
     da.cpix = pa.out.cpix;
-    da.queue = (const int *)ctx->queue.p;
+    da.queue = (const int *)ctx->w->queue.p;
     da.ctr = pa.ctr;
     da.acc = acc;
     if (ctx->precision == DMANN_COMP_F32) da.chdr = headers_for(ctx, N);
@@ -868,8 +886,8 @@ dmann_status dmann_map_end(dmann_ctx *ctx, double *map_out, int accumulate) {
                        accumulate, s));
     ctx->launches++;
     CK(cudaEventRecord(ctx->ev1, s));
-    CK(cudaMemcpyAsync(ctx->h_ctr, ctx->ctr.p, 8 * C_COUNT, cudaMemcpyDeviceToHost, s));
-    CK(cudaMemcpyAsync(ctx->h_fsum, ctx->fsum.p, 8, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(ctx->h_ctr, ctx->w->ctr.p, 8 * C_COUNT, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(ctx->h_fsum, ctx->w->fsum.p, 8, cudaMemcpyDeviceToHost, s));
     ctx->stats_pending = true;
     ctx->in_map = false;
     if (!map_dev) {
@@ -917,13 +935,11 @@ namespace {
 // Adds one observer's counters into the batch's sums (ctx->bstats: kept,
 // invalid, single, disc, block-class, deposits, then the kept flux).
 __global__ void k_batch_stats(const long long *ctr, const double *fsum, long long *out) {
-    out[0] += ctr[C_KEPT];
-    out[1] += ctr[C_INVALID];
-    out[2] += ctr[C_SINGLE];
-    out[3] += ctr[C_DISC];
-    out[4] += ctr[C_DISC_BLOCK];
-    out[5] += ctr[C_DEPOSITS];
-    reinterpret_cast<double *>(out)[6] += *fsum;
+    // atomics: the two lanes of a batch add concurrently
+    const int idx[6] = {C_KEPT, C_INVALID, C_SINGLE, C_DISC, C_DISC_BLOCK, C_DEPOSITS};
+    for (int i = 0; i < 6; i++)
+        atomicAdd(reinterpret_cast<unsigned long long *>(out) + i, (unsigned long long)ctr[idx[i]]);
+    atomicAdd(reinterpret_cast<double *>(out) + 6, *fsum);
 }
 
 constexpr int kBatchStats = 7;
@@ -934,33 +950,33 @@ dmann_status issue_observer(dmann_ctx *ctx, const float *const dev[6], int n, in
     ctx->g = make_hpx(nside);
     ctx->precision = precision;
     const size_t P = (size_t)ctx->g.npix;
-    CK(cudaMemsetAsync(ctx->acc.p, 0, 8 * P, s));
-    CK(cudaMemsetAsync(ctx->ctr.p, 0, 8 * C_COUNT, s));
-    CK(cudaMemsetAsync(ctx->fsum.p, 0, 8, s));
+    CK(cudaMemsetAsync(ctx->w->acc.p, 0, 8 * P, s));
+    CK(cudaMemsetAsync(ctx->w->ctr.p, 0, 8 * C_COUNT, s));
+    CK(cudaMemsetAsync(ctx->w->fsum.p, 0, 8, s));
     double scale;
     const Frame f = make_frame(ctx, &scale);
     const Accum acc = make_accum(ctx);
     if (n > 0) {
         const dmann_tuning &tu = tuning_for(ctx, nside);
         const int bmin = block_bucket_min(tu);
-        CK(cudaMemsetAsync(ctx->hist.p, 0, 4 * (size_t)kKeys, s));
+        CK(cudaMemsetAsync(ctx->w->hist.p, 0, 4 * (size_t)kKeys, s));
         PrepArgs pa;
         pa.p = {dev[0], dev[1], dev[2], dev[3], dev[4], dev[5], n};
         pa.core_corr = (const double *)ctx->corr.p;   // filled once per batch (core law)
         pa.f = f;
         pa.g = ctx->g;
-        pa.out = {(double *)ctx->theta.p, (double *)ctx->phi.p, (double *)ctx->ar.p,
-                  (double *)ctx->flux.p, (int *)ctx->cpix.p, (int *)ctx->key.p};
-        pa.hist = (int *)ctx->hist.p;
-        pa.ctr = (long long *)ctx->ctr.p;
-        pa.flux_sum = (double *)ctx->fsum.p;
+        pa.out = {(double *)ctx->w->theta.p, (double *)ctx->w->phi.p, (double *)ctx->w->ar.p,
+                  (double *)ctx->w->flux.p, (int *)ctx->w->cpix.p, (int *)ctx->w->key.p};
+        pa.hist = (int *)ctx->w->hist.p;
+        pa.ctr = (long long *)ctx->w->ctr.p;
+        pa.flux_sum = (double *)ctx->w->fsum.p;
         pa.acc = acc;
         pa.precision = precision;
         pa.block_bucket_min = bmin;
         pa.deposit_singles = 1;
         CK(launch_prep(pa, s));
         CK(launch_scan(pa.hist, pa.ctr, bmin, s));
-        CK(launch_scatter(pa, (int *)ctx->queue.p, s));
+        CK(launch_scatter(pa, (int *)ctx->w->queue.p, s));
         DiscArgs da;
         da.g = ctx->g;
         da.f = f;
@@ -970,7 +986,7 @@ dmann_status issue_observer(dmann_ctx *ctx, const float *const dev[6], int n, in
         da.ar = pa.out.ar;
         da.flux = pa.out.flux;
         da.cpix = pa.out.cpix;
-        da.queue = (const int *)ctx->queue.p;
+        da.queue = (const int *)ctx->w->queue.p;
         da.ctr = pa.ctr;
         da.acc = acc;
         if (precision == DMANN_PLAIN_F64) {
@@ -984,7 +1000,7 @@ dmann_status issue_observer(dmann_ctx *ctx, const float *const dev[6], int n, in
         }
     }
     CK(launch_finalize(acc, precision, ctx->g.npix, ctx->g.dOmega, scale, dmap, 0, s));
-    k_batch_stats<<<1, 1, 0, s>>>((const long long *)ctx->ctr.p, (const double *)ctx->fsum.p,
+    k_batch_stats<<<1, 1, 0, s>>>((const long long *)ctx->w->ctr.p, (const double *)ctx->w->fsum.p,
                                   (long long *)ctx->bstats.p);
     CK(cudaGetLastError());
     return DMANN_OK;
@@ -1021,23 +1037,47 @@ dmann_status dmann_render_batch(dmann_ctx *ctx, const float *x, const float *y, 
     if ((st = collect_stats(ctx)) != DMANN_OK) return st;
     cudaStream_t s = ctx->stream;
     const size_t N = (size_t)n, n1 = N > 0 ? N : 1, Pmax = 12 * (size_t)maxns * (size_t)maxns;
-    // everything is sized and uploaded before the observers are issued
-    if ((st = ensure(ctx, ctx->theta, 8 * n1)) || (st = ensure(ctx, ctx->phi, 8 * n1)) ||
-        (st = ensure(ctx, ctx->ar, 8 * n1)) || (st = ensure(ctx, ctx->flux, 8 * n1)) ||
-        (st = ensure(ctx, ctx->cpix, 4 * n1)) || (st = ensure(ctx, ctx->key, 4 * n1)) ||
-        (st = ensure(ctx, ctx->queue, 4 * n1)) || (st = ensure(ctx, ctx->hist, 4 * (size_t)kKeys)) ||
-        (st = ensure(ctx, ctx->ctr, 8 * C_COUNT)) || (st = ensure(ctx, ctx->fsum, 8)) ||
-        (st = ensure(ctx, ctx->acc, 8 * Pmax)) || (st = ensure(ctx, ctx->map, 8 * Pmax)))
-        return st;
-    if ((st = ensure(ctx, ctx->bstats, 8 * kBatchStats)) != DMANN_OK) return st;
-    // before any capture: the disc headers and the segmented render's buffers
-    // (the render checks them again and allocates nothing when they fit)
-    ctx->seg_plane = false;
-    if (precision == DMANN_COMP_F32) {
-        reserve_headers(ctx, n1);
-        ctx->seg_plane = ensure_opt(ctx->plane32, 4 * Pmax) && reserve_seg(ctx, N);
-        if (ctx->seg_plane) CK(cudaMemsetAsync(ctx->plane32.p, 0, 4 * Pmax, s));
+    // device maps: the observers alternate between two workspaces (lanes),
+    // each on its own stream in the captured graph, so one observer's prep and
+    // the tails of its passes overlap the other's work
+    std::vector<char> on_dev(n_obs);
+    bool all_dev = true;
+    for (int k = 0; k < n_obs; k++) all_dev &= (on_dev[k] = is_device_ptr(maps[k])) != 0;
+    int lanes = (all_dev && n_obs > 1) ? 2 : 1;
+    if (lanes == 2 && !ctx->lane_stream &&
+        (cudaStreamCreateWithFlags(&ctx->lane_stream, cudaStreamNonBlocking) != cudaSuccess ||
+         cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+         cudaEventCreateWithFlags(&ctx->ev_join, cudaEventDisableTiming) != cudaSuccess)) {
+        cudaGetLastError();
+        lanes = 1;
     }
+    // everything is sized and uploaded before the observers are issued
+    if ((st = ensure(ctx, ctx->map, 8 * Pmax)) || (st = ensure(ctx, ctx->bstats, 8 * kBatchStats))) return st;
+    for (int L = 0; L < lanes; L++) {
+        ctx->w = &ctx->work[L];
+        st = DMANN_OK;
+        if ((st = ensure(ctx, ctx->w->theta, 8 * n1)) || (st = ensure(ctx, ctx->w->phi, 8 * n1)) ||
+            (st = ensure(ctx, ctx->w->ar, 8 * n1)) || (st = ensure(ctx, ctx->w->flux, 8 * n1)) ||
+            (st = ensure(ctx, ctx->w->cpix, 4 * n1)) || (st = ensure(ctx, ctx->w->key, 4 * n1)) ||
+            (st = ensure(ctx, ctx->w->queue, 4 * n1)) || (st = ensure(ctx, ctx->w->hist, 4 * (size_t)kKeys)) ||
+            (st = ensure(ctx, ctx->w->ctr, 8 * C_COUNT)) || (st = ensure(ctx, ctx->w->fsum, 8)) ||
+            (st = ensure(ctx, ctx->w->acc, 8 * Pmax))) {
+            ctx->w = &ctx->work[0];
+            if (L == 0) return st;
+            lanes = 1;   // no room for a second workspace: one lane
+            break;
+        }
+        // before any capture: the disc headers and the segmented render's
+        // buffers (the render checks them again and allocates nothing when
+        // they fit)
+        ctx->w->seg_plane = false;
+        if (precision == DMANN_COMP_F32) {
+            reserve_headers(ctx, n1);
+            ctx->w->seg_plane = ensure_opt(ctx->w->plane32, 4 * Pmax) && reserve_seg(ctx, N);
+            if (ctx->w->seg_plane) CK(cudaMemsetAsync(ctx->w->plane32.p, 0, 4 * Pmax, s));
+        }
+    }
+    ctx->w = &ctx->work[0];
     std::vector<RingTables> rts(n_obs);
     for (int k = 0; k < n_obs; k++)
         if ((st = ring_tables(ctx, nside[k], rts[k])) != DMANN_OK) return st;
@@ -1058,9 +1098,6 @@ dmann_status dmann_render_batch(dmann_ctx *ctx, const float *x, const float *y, 
         Particles pp = {dev[0], dev[1], dev[2], dev[3], dev[4], dev[5], (int)N};
         CK(launch_halo_core(ctx->halo, pp, (double *)ctx->corr.p, nullptr, s));
     }
-    std::vector<char> on_dev(n_obs);
-    bool all_dev = true;
-    for (int k = 0; k < n_obs; k++) all_dev &= (on_dev[k] = is_device_ptr(maps[k])) != 0;
     // the parameters a captured graph depends on: a batch that repeats them
     // relaunches the cached graph instead of capturing again
     std::vector<char> key;
@@ -1082,7 +1119,8 @@ dmann_status dmann_render_batch(dmann_ctx *ctx, const float *x, const float *y, 
     put(&ctx->flux_model, sizeof ctx->flux_model);
     put(&ctx->vel_to_cgs, sizeof ctx->vel_to_cgs);
     put(ctx->fcpos, sizeof ctx->fcpos);
-    put(&ctx->seg_plane, sizeof ctx->seg_plane);
+    put(&lanes, sizeof lanes);
+    for (int L = 0; L < lanes; L++) put(&ctx->work[L].seg_plane, sizeof(bool));
     for (int k = 0; k < n_obs; k++) put(&tuning_for(ctx, nside[k]), sizeof(dmann_tuning));
     double rot0[9], opos0[3];
     std::memcpy(rot0, ctx->rot, sizeof rot0);
@@ -1112,11 +1150,21 @@ dmann_status dmann_render_batch(dmann_ctx *ctx, const float *x, const float *y, 
         }
         cudaError_t e = cudaMemsetAsync(ctx->bstats.p, 0, 8 * kBatchStats, s);
         if (e != cudaSuccess) st = fail(ctx, DMANN_ERR_CUDA, std::string("batch: ") + cudaGetErrorString(e));
+        if (st == DMANN_OK && lanes == 2) {   // the second lane joins the capture
+            e = cudaEventRecord(ctx->ev_fork, s);
+            if (e == cudaSuccess) e = cudaStreamWaitEvent(ctx->lane_stream, ctx->ev_fork, 0);
+            if (e != cudaSuccess) st = fail(ctx, DMANN_ERR_CUDA, std::string("batch fork: ") + cudaGetErrorString(e));
+        }
         for (int k = 0; k < n_obs && st == DMANN_OK; k++) {
             std::memcpy(ctx->rot, rot + 9 * k, sizeof(double) * 9);
             std::memcpy(ctx->opos, opos + 3 * k, sizeof(double) * 3);
             double *dmap = on_dev[k] ? maps[k] : (double *)ctx->map.p;
+            const int L = k % lanes;
+            ctx->w = &ctx->work[L];
+            ctx->stream = L == 0 ? s : ctx->lane_stream;
             st = issue_observer(ctx, dev, (int)N, nside[k], rts[k], precision, dmap);
+            ctx->w = &ctx->work[0];
+            ctx->stream = s;
             if (st == DMANN_OK && !on_dev[k]) {
                 const size_t P = 12 * (size_t)nside[k] * (size_t)nside[k];
                 e = cudaMemcpyAsync(maps[k], dmap, 8 * P, cudaMemcpyDeviceToHost, s);
@@ -1128,6 +1176,12 @@ dmann_status dmann_render_batch(dmann_ctx *ctx, const float *x, const float *y, 
         std::memcpy(ctx->opos, opos0, sizeof opos0);
         ctx->have_frame = had_frame;
         ctx->have_geom = had_geom;
+        if (lanes == 2) {   // join the second lane before the capture ends
+            cudaError_t ej = cudaEventRecord(ctx->ev_join, ctx->lane_stream);
+            if (ej == cudaSuccess) ej = cudaStreamWaitEvent(s, ctx->ev_join, 0);
+            if (ej != cudaSuccess && st == DMANN_OK)
+                st = fail(ctx, DMANN_ERR_CUDA, std::string("batch join: ") + cudaGetErrorString(ej));
+        }
         if (all_dev) {
             e = cudaStreamEndCapture(s, &graph);
             ctx->stream = caller;
@@ -1226,17 +1280,17 @@ dmann_status dmann_adjoint_v(dmann_ctx *ctx, const float *x, const float *y, con
     const size_t N = (size_t)n, n1 = N > 0 ? N : 1, P = (size_t)g.npix;
     RingTables rt;
     if ((st = ring_tables(ctx, nside, rt)) != DMANN_OK) return st;
-    if ((st = ensure(ctx, ctx->theta, 8 * n1)) || (st = ensure(ctx, ctx->phi, 8 * n1)) ||
-        (st = ensure(ctx, ctx->ar, 8 * n1)) || (st = ensure(ctx, ctx->flux, 8 * n1)) ||
-        (st = ensure(ctx, ctx->cpix, 4 * n1)) || (st = ensure(ctx, ctx->key, 4 * n1)) ||
-        (st = ensure(ctx, ctx->queue, 4 * n1)) || (st = ensure(ctx, ctx->cls, n1)) ||
-        (st = ensure(ctx, ctx->hist, 4 * (size_t)kKeys)) || (st = ensure(ctx, ctx->ctr, 8 * C_COUNT)) ||
-        (st = ensure(ctx, ctx->fsum, 8)) || (st = ensure(ctx, ctx->oacc, 8 * 12)))
+    if ((st = ensure(ctx, ctx->w->theta, 8 * n1)) || (st = ensure(ctx, ctx->w->phi, 8 * n1)) ||
+        (st = ensure(ctx, ctx->w->ar, 8 * n1)) || (st = ensure(ctx, ctx->w->flux, 8 * n1)) ||
+        (st = ensure(ctx, ctx->w->cpix, 4 * n1)) || (st = ensure(ctx, ctx->w->key, 4 * n1)) ||
+        (st = ensure(ctx, ctx->w->queue, 4 * n1)) || (st = ensure(ctx, ctx->cls, n1)) ||
+        (st = ensure(ctx, ctx->w->hist, 4 * (size_t)kKeys)) || (st = ensure(ctx, ctx->w->ctr, 8 * C_COUNT)) ||
+        (st = ensure(ctx, ctx->w->fsum, 8)) || (st = ensure(ctx, ctx->oacc, 8 * 12)))
         return st;
     if (core && ((st = ensure(ctx, ctx->corr, 8 * n1)) || (st = ensure(ctx, ctx->core_gln, 24 * n1))))
         return st;
     if (precision == DMANN_COMP_F32) {
-        if ((st = ensure(ctx, ctx->acc, 4 * P)) != DMANN_OK) return st;
+        if ((st = ensure(ctx, ctx->w->acc, 4 * P)) != DMANN_OK) return st;
         reserve_headers(ctx, n1);
     }
     const float *src[7] = {x, y, z, m, rho, h, law_needs_sigmav(ctx->flux_model) ? sigmav : nullptr};
@@ -1267,20 +1321,20 @@ dmann_status dmann_adjoint_v(dmann_ctx *ctx, const float *x, const float *y, con
     const Frame f = make_frame(ctx, &scale);
     const int bmin = block_bucket_min(ctx->tune);
     CK(cudaEventRecord(ctx->ev0, s));
-    CK(cudaMemsetAsync(ctx->ctr.p, 0, 8 * C_COUNT, s));
-    CK(cudaMemsetAsync(ctx->fsum.p, 0, 8, s));
+    CK(cudaMemsetAsync(ctx->w->ctr.p, 0, 8 * C_COUNT, s));
+    CK(cudaMemsetAsync(ctx->w->fsum.p, 0, 8, s));
     CK(cudaMemsetAsync(ctx->oacc.p, 0, 8 * 12, s));
-    CK(cudaMemsetAsync(ctx->hist.p, 0, 4 * (size_t)kKeys, s));
+    CK(cudaMemsetAsync(ctx->w->hist.p, 0, 4 * (size_t)kKeys, s));
     PrepArgs pa;
     pa.p = {dev[0], dev[1], dev[2], dev[3], dev[4], dev[5], (int)N, dev[6]};
     pa.f = f;
     pa.g = g;
-    pa.out = {(double *)ctx->theta.p, (double *)ctx->phi.p, (double *)ctx->ar.p,
-              (double *)ctx->flux.p, (int *)ctx->cpix.p, (int *)ctx->key.p,
+    pa.out = {(double *)ctx->w->theta.p, (double *)ctx->w->phi.p, (double *)ctx->w->ar.p,
+              (double *)ctx->w->flux.p, (int *)ctx->w->cpix.p, (int *)ctx->w->key.p,
               (signed char *)ctx->cls.p};
-    pa.hist = (int *)ctx->hist.p;
-    pa.ctr = (long long *)ctx->ctr.p;
-    pa.flux_sum = (double *)ctx->fsum.p;
+    pa.hist = (int *)ctx->w->hist.p;
+    pa.ctr = (long long *)ctx->w->ctr.p;
+    pa.flux_sum = (double *)ctx->w->fsum.p;
     pa.acc = Accum{nullptr};
     pa.precision = DMANN_PLAIN_F64;
     pa.block_bucket_min = bmin;
@@ -1292,7 +1346,7 @@ dmann_status dmann_adjoint_v(dmann_ctx *ctx, const float *x, const float *y, con
     }
     CK(launch_prep(pa, s));
     CK(launch_scan(pa.hist, pa.ctr, bmin, s));
-    CK(launch_scatter(pa, (int *)ctx->queue.p, s));
+    CK(launch_scatter(pa, (int *)ctx->w->queue.p, s));
     DiscArgs da;
     da.g = g;
     da.f = f;
@@ -1302,20 +1356,20 @@ dmann_status dmann_adjoint_v(dmann_ctx *ctx, const float *x, const float *y, con
     da.ar = pa.out.ar;
     da.flux = pa.out.flux;
     da.cpix = pa.out.cpix;
-    da.queue = (const int *)ctx->queue.p;
+    da.queue = (const int *)ctx->w->queue.p;
     da.ctr = pa.ctr;
     da.acc = pa.acc;
     if (precision == DMANN_COMP_F32) da.chdr = headers_for(ctx, n1);
     CK(cudaEventRecord(ctx->evd0, s));
-    CK(launch_adjoint(da, pa.p, pa.out.cls, dgmap, (float *)ctx->acc.p, dgrad, (double *)ctx->oacc.p,
+    CK(launch_adjoint(da, pa.p, pa.out.cls, dgmap, (float *)ctx->w->acc.p, dgrad, (double *)ctx->oacc.p,
                       precision, ctx->num_sms, s, core ? (const double *)ctx->corr.p : nullptr,
                       core ? (const double *)ctx->core_gln.p : nullptr));
     CK(cudaEventRecord(ctx->evd1, s));
     CK(cudaEventRecord(ctx->evdm, s));
     CK(cudaEventRecord(ctx->ev1, s));
     if (!grad_dev && N > 0) CK(cudaMemcpyAsync(grad, dgrad, 48 * N, cudaMemcpyDeviceToHost, s));
-    CK(cudaMemcpyAsync(ctx->h_ctr, ctx->ctr.p, 8 * C_COUNT, cudaMemcpyDeviceToHost, s));
-    CK(cudaMemcpyAsync(ctx->h_fsum, ctx->fsum.p, 8, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(ctx->h_ctr, ctx->w->ctr.p, 8 * C_COUNT, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(ctx->h_fsum, ctx->w->fsum.p, 8, cudaMemcpyDeviceToHost, s));
     CK(cudaMemcpyAsync(ctx->h_oacc, ctx->oacc.p, 8 * 12, cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
     ctx->stats = dmann_stats{};

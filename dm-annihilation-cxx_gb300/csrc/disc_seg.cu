@@ -242,12 +242,12 @@ __device__ inline void seg_walk_any(SegSmem<RCH> &sm, int n, Body body, Done rin
     else seg_walk_block<BT, RCH>(sm, n, body, ring_done);
 }
 
-// Lanes per ring.  Pass 1 (weights only) walks eight rings per warp: measured
-// on the 16M workload at Nside 2048, 4 / 8 / 16 / 32 lanes per ring took
-// 435 / 460 / 519 / 627 ms.  Pass 2 keeps whole warps on a ring, so a warp's
+// Lanes per ring.  Pass 1 (weights only) walks sixteen rings per warp:
+// measured on the 16M workload at Nside 2048, 2 / 4 / 8 / 16 / 32 lanes per
+// ring took 413 / 418 / 460 / 519 / 627 ms.  Pass 2 keeps whole warps on a ring, so a warp's
 // reduction covers 32 consecutive floats: 16 lanes per ring, or eight lanes
 // on aligned 32-byte sectors, measured slower (760 and 826 ms against 753).
-constexpr int kNormLanes = 4;
+constexpr int kNormLanes = 2;
 constexpr int kDepLanes = 32;
 constexpr int kFoldPairs = 8;    // pass 1, large discs: pixel pairs per plain FP32 partial
 
