@@ -18,9 +18,6 @@ constexpr int kCells = 1 << kCellBits;
 constexpr int kBuckets = 32;
 constexpr int kKeys = kBuckets * kCells;
 
-// Device counters (int64).  The first six accumulate over every chunk of
-// a map; the C_ADD_* ones describe the chunk being added and are reset for
-// each chunk.
 // Segmented render (disc_seg.cu).  The items are sorted into kClasses
 // octaves of their disc's deposit scale; a segment of deposits spans at most
 // kClassSpan consecutive octaves and about kDepPerPix FP32 additions per
@@ -40,6 +37,9 @@ constexpr size_t kSegNextBytes = 8 * kSegSlots;
 constexpr size_t kSegSpanBytes = 24 * kSegSlots;
 constexpr size_t kSegBufBytes = kSegClsBytes + kSegClsPxBytes + kSegNextBytes + kSegSpanBytes + 16;
 
+// Device counters (int64).  The first six accumulate over every chunk of
+// a map; the ones from C_ADD_DISC on describe the chunk being added and are
+// reset for each chunk.
 enum Ctr {
     C_KEPT = 0, C_SINGLE, C_DISC, C_DISC_BLOCK, C_DEPOSITS, C_INVALID,
     C_ADD_DISC, C_ADD_BLOCK, C_QNEXT_BLOCK, C_QNEXT_WARP,
