@@ -526,56 +526,10 @@ __global__ void __launch_bounds__(256) k_seg_sort(DiscArgs a, SegArgs sg) {
     }
 }
 
-// The segment plan from the per-octave histograms (one thread): n[c] items
-// ending at slot end[c] of the sorted list (k_seg_sort leaves each octave's
-// end slot), px[c] deposits.  Consecutive octaves are grouped while the
-// group spans at most kClassSpan octaves and budget deposits; an octave with
-// more than budget deposits is dealt round robin into ceil(px / budget)
-// segments of its own.  Class 0 (discs with no weighted deposits: single
-// pixels, zero flux) is one segment.  At most kSegSlots segments: the budget
-// doubles until the plan fits.
+// The segment plan (plan_segments in seg_plan.h), one thread.
 __global__ void k_seg_plan(SegArgs sg) {
     if (sg.ctl[0] == 0) return;
-    const int *n = sg.cls, *end = sg.cls + kClasses;
-    const long long *px = sg.cls_px;
-    for (long long budget = max(1LL, sg.budget);; budget *= 2) {
-        int ns = 0;
-        auto push = [&](long long lo, long long hi, int stride, int offset) {
-            if (ns < kSegSlots) sg.spans[ns] = SegSpan{lo, hi, stride, offset};
-            ns++;
-        };
-        if (n[0] > 0) push((long long)end[0] - n[0], end[0], 1, 0);
-        int c0 = -1;
-        long long lo = 0, hi = 0, acc = 0;
-        for (int c = 1; c < kClasses; ++c) {
-            if (n[c] == 0) continue;
-            const long long f = (long long)end[c] - n[c];
-            if (px[c] > budget) {
-                if (c0 >= 0) push(lo, hi, 1, 0);
-                c0 = -1;
-                acc = 0;
-                const long long m = min((long long)n[c], (px[c] + budget - 1) / budget);
-                for (long long k = 0; k < m; ++k) push(f, end[c], (int)m, (int)k);
-                continue;
-            }
-            if (c0 >= 0 && (c - c0 >= kClassSpan || acc + px[c] > budget)) {
-                push(lo, hi, 1, 0);
-                c0 = -1;
-                acc = 0;
-            }
-            if (c0 < 0) {
-                c0 = c;
-                lo = f;
-            }
-            hi = end[c];
-            acc += px[c];
-        }
-        if (c0 >= 0) push(lo, hi, 1, 0);
-        if (ns <= kSegSlots) {
-            sg.ctl[1] = ns;
-            return;
-        }
-    }
+    sg.ctl[1] = plan_segments(sg.cls, sg.cls + kClasses, sg.cls_px, sg.budget, sg.spans);
 }
 
 // After segment seg: acc64 += plane, plane = 0 (four pixels per thread;

@@ -5,6 +5,7 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 #include "common.cuh"
+#include "seg_plan.h"
 
 namespace dmann {
 
@@ -18,18 +19,12 @@ constexpr int kCells = 1 << kCellBits;
 constexpr int kBuckets = 32;
 constexpr int kKeys = kBuckets * kCells;
 
-// Segmented render (disc_seg.cu).  The items are sorted into kClasses
-// octaves of their disc's deposit scale; a segment of deposits spans at most
-// kClassSpan consecutive octaves and about kDepPerPix FP32 additions per
-// pixel, with kSegSlots segments at most per chunk (the plan is made on the
-// device; each chunk launches kSegSlots deposit/flush pairs, the unused ones
-// return at once).  Chunks whose estimated deposits are below
-// 2^seg_min_deposits_log2 (a tunable), or whose work items exceed the item
-// buffers, deposit in FP64 with the per-disc kernels.
-constexpr int kClasses = 256;
-constexpr int kClassSpan = 2;
-constexpr int kDepPerPix = 512;
-constexpr int kSegSlots = 64;
+// Segmented render (disc_seg.cu; its constants and segment plan are in
+// seg_plan.h).  The plan is made on the device; each chunk launches
+// kSegSlots deposit/flush pairs, the unused ones return at once.  Chunks
+// whose estimated deposits are below 2^seg_min_deposits_log2 (a tunable), or
+// whose work items exceed the item buffers, deposit in FP64 with the per-disc
+// kernels.
 // The segment buffer, zeroed per chunk: cls, cls_px, seg_next, spans, ctl.
 constexpr size_t kSegClsBytes = 2 * 4 * kClasses;
 constexpr size_t kSegClsPxBytes = 8 * kClasses;
@@ -118,13 +113,7 @@ struct DiscArgs {
     const int *block_skip = nullptr;
 };
 
-// One segment of deposits: items lo + offset, lo + offset + stride, ... below
-// hi of the sorted list.
-struct SegSpan {
-    long long lo, hi;
-    int stride, offset;
-};
-static_assert(sizeof(SegSpan) == 24, "the segment buffer holds 24-byte spans");
+
 
 // Segmented render of the block-class discs (disc_seg.cu).
 struct SegArgs {
