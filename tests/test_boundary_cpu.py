@@ -184,3 +184,29 @@ def test_flux_unit_factors_match_oracle():
         assert par.flux_unit_factor(law) == p.unit_factor == par.unit_factor
     with pytest.raises(ValueError):
         par.flux_unit_factor(9)
+
+
+def test_struct_layouts_match_the_header(tmp_path):
+    """The ctypes mirrors of dmann_stats and dmann_tuning have the header's
+    field names, offsets and sizes (a C program compiled against dmann.h
+    prints them)."""
+    import subprocess
+    mirrors = {"dmann_stats": _lib.Stats, "dmann_tuning": _lib.Tuning}
+    lines = ['#include <stddef.h>', '#include <stdio.h>', '#include "dmann.h"', "int main(void) {"]
+    for cname, py in mirrors.items():
+        lines.append(f'    printf("{cname} size %zu\\n", sizeof({cname}));')
+        for field, _ in py._fields_:
+            lines.append(f'    printf("{cname} {field} %zu\\n", offsetof({cname}, {field}));')
+    lines += ["    return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = str(tmp_path / "layout")
+    subprocess.run(["gcc", "-std=c11", "-I", os.path.join(REPO, "include"), str(src), "-o", exe], check=True)
+    got = {}
+    for ln in subprocess.run([exe], capture_output=True, text=True, check=True).stdout.splitlines():
+        cname, field, val = ln.split()
+        got[(cname, field)] = int(val)
+    for cname, py in mirrors.items():
+        assert got[(cname, "size")] == C.sizeof(py), cname
+        for field, _ in py._fields_:
+            assert got[(cname, field)] == getattr(py, field).offset, (cname, field)
