@@ -51,6 +51,8 @@ def parse():
                     "workload's (the overlap density, deposits per pixel, does not depend on it)")
     ap.add_argument("--plain-scale", type=float, default=1.0 / 64)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--ref-seconds", type=float, default=60.0, help="reference arm: timed CPU seconds "
+                    "over all steps")
     ap.add_argument("--no-extras", action="store_true", help="skip plain form, e2e and CPU legs")
     ap.add_argument("--no-tune", action="store_true", help="keep the default tuning (no autotuner)")
     return ap.parse_args()
@@ -257,7 +259,7 @@ def run_reference(args, ws, rank):
     """The reference arm: the CPU restatement of the reference's own map path
     (src/genmap.cpp) on every host thread, on the same workload.  Each step
     renders a different slice of the shuffled (hence i.i.d.) particle set,
-    sized so that the timed steps take about 60 s together; particles/s and
+    sized so that the timed steps take about --ref-seconds (60 s) together; particles/s and
     deposits/s are totals over the timed slices, and ms_per_step is the time
     the whole set would take at that rate (an extrapolation)."""
     if rank != 0:
@@ -275,7 +277,7 @@ def run_reference(args, ws, rank):
                       particle_masses=(P.particle_mass,))
     # a calibration slice, then slices of about `per_step` seconds (warm-up
     # steps a tenth of that)
-    per_step = min(20.0, max(3.0, 60.0 / max(1, args.steps)))
+    per_step = min(20.0, max(min(3.0, args.ref_seconds), args.ref_seconds / max(1, args.steps)))
     k0 = min(n, 64 * threads)
     t0 = time.perf_counter()
     O.render(o, P.subset(slice(0, k0)).as_dict(), nthreads=threads, finalize=False)
