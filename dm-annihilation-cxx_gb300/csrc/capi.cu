@@ -663,7 +663,10 @@ Accum make_accum(dmann_ctx *ctx) {
 // captured in a graph.  Needs the disc headers, the FP32 plane and the item
 // buffers; without them `used` stays false and the caller renders with the
 // per-disc kernels alone.
-size_t seg_capacity(size_t n) { return 4 * (n > 0 ? n : 1) + ((size_t)1 << 20); }
+// Item slots of the segmented render: 4 n + 2^20 (items are indexed as int).
+size_t seg_capacity(size_t n) {
+    return std::min<size_t>(4 * (n > 0 ? n : 1) + ((size_t)1 << 20), (size_t)0x7fffffff);
+}
 
 // The segmented render's buffers for chunks of n particles (optional: false
 // when an allocation fails; nothing is allocated when they are big enough).
