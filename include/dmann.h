@@ -239,7 +239,9 @@ dmann_status dmann_map_add_v(dmann_ctx *ctx, const float *x, const float *y,
  * the frame rot[9k..9k+8] / opos[3k..3k+2] (as dmann_set_frame) and its own
  * nside[k]; its map goes to maps[k] (12*nside[k]^2 doubles, host or device).
  * The particles are uploaded once; when every map is a device pointer the
- * whole batch is captured into one CUDA graph and launched once.  The context
+ * whole batch is captured into one CUDA graph and launched once, the
+ * observers alternating between two workspaces on two streams (the context
+ * keeps a second set of per-particle buffers and planes for that).  The context
  * keeps that graph: a later batch with the same inputs, maps, frames, Nside
  * values, units and tuning (and no context buffer reallocated since) launches
  * it again without capturing; one with other frames or maps updates it in
