@@ -56,7 +56,8 @@
 //     octave with more is dealt round robin into several segments), so a
 //     pixel's FP32 partial sums stay short and their rounding errors random.
 // The plan is made on the device from the per-octave histograms
-// (k_seg_plan), and every kernel of the sequence reads the chunk's mode
+// (k_seg_plan, running plan_segments of seg_plan.h), and every kernel of the
+// sequence reads the chunk's mode
 // (k_seg_decide) and returns at once when it has nothing to do, so the
 // whole render is one stream of launches with no host synchronisation.
 // Chunks too small for the L2 reduction rate to matter (a tunable threshold
